@@ -1,0 +1,73 @@
+"""GB300-native approximate discrete Radon transform (ADRT).
+
+A drop-in for the public API of the ``adrt`` package (karlotness/adrt):
+``adrt``, ``bdrt``, ``iadrt``, ``iadrt_fmg``, ``adrt_gb300.core`` and
+``adrt_gb300.utils``, computed by hand-written sm_103a CUDA kernels behind the
+C ABI in include/adrt_gb300.h.  Inputs may be CUDA tensors (results stay on
+the device) or host arrays (NumPy / CPU tensors: copied in and out).
+There is no CPU compute path.
+"""
+
+from __future__ import annotations
+
+import collections.abc
+import itertools
+import math
+import typing
+
+import numpy as np
+import torch
+
+from . import core, utils
+from . import _lib
+from ._ops import adrt, bdrt, iadrt
+from ._wrappers import Staged, float_code, ptr
+
+__all__: typing.Final[collections.abc.Sequence[str]] = [
+    "adrt",
+    "iadrt",
+    "bdrt",
+    "iadrt_fmg",
+    "utils",
+    "core",
+]
+
+__version__: typing.Final[str] = "0.1.0"
+
+
+def _residual_norm(x: torch.Tensor, a: torch.Tensor, ws: torch.Tensor, acc: torch.Tensor) -> float:
+    """||adrt(x) - a||_2 accumulated in float64 on the device."""
+    r = core._sub(adrt(x), a)
+    rc = _lib.load().adrt_gb300_sumsq(
+        ptr(r), r.numel(), float_code(r), ptr(acc), ptr(ws), torch.cuda.current_stream(r.device).cuda_stream
+    )
+    _lib.check(rc, "sumsq")
+    return math.sqrt(float(acc.item()))
+
+
+def iadrt_fmg(a, /, *, max_iters: int | None = None):
+    """Approximate inverse of the ADRT by the full multigrid method, refined
+    until the residual norm stops decreasing or `max_iters` estimates were made.
+    No batch dimension.  Reference: src/adrt/__init__.py:69-148 (same iteration
+    and stopping rule; the residual norm is accumulated in float64)."""
+    if a.ndim > 3:
+        raise ValueError(f"batch dimension not supported for iadrt_fmg, got {a.ndim} dimensions")
+    if max_iters is not None and max_iters < 1:
+        raise ValueError(f"must allow at least one iteration, but specified {max_iters}")
+    st = Staged(a)
+    t = st.t
+    ws = torch.empty(_lib.load().adrt_gb300_sumsq_workspace_size(), dtype=torch.uint8, device=st.device)
+    acc = torch.empty((), dtype=torch.float64, device=st.device)
+    inv1 = t
+    for (inv1, res1), (_, res2) in itertools.pairwise(
+        itertools.chain(
+            (
+                (x, _residual_norm(x, t, ws, acc))
+                for x in itertools.islice(core.iadrt_fmg_iter(t, copy=False), max_iters)
+            ),
+            [(t, np.inf)],
+        )
+    ):
+        if not res2 < res1:
+            break
+    return st.finish(inv1.clone())

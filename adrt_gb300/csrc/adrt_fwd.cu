@@ -1,0 +1,244 @@
+// Forward ADRT: fused multi-stage passes.
+//
+// The reference runs log2(n) butterfly stages over a per-quadrant buffer of
+// shape [R][A][2n-1] (rows, angles, offsets), each stage
+//   out[r][a][c] = in[2r][a/2][c] + in[2r+1][a/2][c - ceil(a/2)]   (c >= ceil(a/2))
+//   out[r][a][c] = in[2r][a/2][c]                                   (otherwise)
+// (src/adrt/adrt_cdefs_adrt.hpp:56-96), after flipping the image into four
+// quadrants (:123-186) and before transposing to (4, 2n-1, n) (:195-210).
+//
+// Here the stages are grouped into passes of S <= 5 stages.  One CTA of a pass
+// owns 2^S consecutive input rows (row groups) at one input angle a', and a
+// window of W output offsets.  Within the pass, the stage that merges members
+// with local angle l and parity p shifts the odd member by (a' * 2^j + l + p);
+// the part a' * 2^j summed over the pass is a' * i for member i, so member i is
+// loaded already shifted by a' * i and only the small residual shift l + p
+// (< 2^S) remains inside the tile.  The copy-versus-add decision is still made
+// on the reference's own offset index, so every output is the same sequence of
+// adds as in the reference.
+//
+// The first pass reads the image directly (the quadrant flips and the +0 pad
+// are fused into its load); the last pass writes the (4, 2n-1, n) layout
+// directly (the transpose is fused into its store).  Passes in between use a
+// workspace laid out like the reference's buffer: [b][q][R][A][2n-1].
+#include "common.cuh"
+
+namespace adrtg {
+
+constexpr int kFwdW = 128;    // output offsets per tile
+constexpr int kFwdHalo = 32;  // halo columns kept left of the tile (>= 2^S - 1)
+constexpr int kFwdThreads = 256;
+
+struct FwdPassArgs {
+  const void *in;  // image (first pass) or stage-k0 buffer
+  void *out;       // stage-(k0+S) buffer, or final output (last pass)
+  i64 n;           // image side
+  int k0;          // index of the first stage of this pass
+  i64 batch;
+};
+
+template <typename T, int S, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kFwdThreads)
+fwd_pass_kernel(FwdPassArgs args) {
+  constexpr int ROWS = 1 << S;
+  constexpr int TWP = kFwdW + kFwdHalo;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *buf0 = reinterpret_cast<T *>(smem_raw);
+  T *buf1 = buf0 + ROWS * TWP;
+
+  const i64 n = args.n;
+  const i64 C = 2 * n - 1;
+  const int k0 = args.k0;
+  const i64 A_in = i64(1) << k0;            // angles at the pass input
+  const i64 R_in = n >> k0;                 // row groups at the pass input
+  const i64 R_out = R_in >> S;
+  const i64 A_out = A_in << S;
+  const int col_tiles = (int)((C + kFwdW - 1) / kFwdW);
+
+  // Decode the tile: (b, q, r, a', column tile), column tile fastest.
+  i64 t = blockIdx.x;
+  const int ct = (int)(t % col_tiles); t /= col_tiles;
+  const i64 ap = t % A_in; t /= A_in;
+  const i64 r = t % R_out; t /= R_out;
+  const int q = (int)(t % 4); t /= 4;
+  const i64 b = t;
+  const i64 c0 = (i64)ct * kFwdW;
+  const i64 tbase = c0 - kFwdHalo;  // reference offset of tile position 0 (before pre-shift)
+
+  // ---- load: member i, tile position u  <->  reference offset tbase + u - a'*i
+  if (FIRST) {
+    const T *img = static_cast<const T *>(args.in) + b * n * n;
+    const bool col_major = (q == 1 || q == 2);
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+      int i, u;
+      if (col_major) { i = idx % ROWS; u = idx / ROWS; }
+      else { i = idx / TWP; u = idx % TWP; }
+      const i64 ref = tbase + u;  // a' == 0 in the first pass
+      const i64 R0 = r * ROWS + i;
+      T v = T(0);
+      if (ref >= 0 && ref < n) {
+        switch (q) {
+          case 0: v = img[R0 * n + (n - 1 - ref)]; break;
+          case 1: v = img[(n - 1 - ref) * n + R0]; break;
+          case 2: v = img[ref * n + R0]; break;
+          default: v = img[(n - 1 - R0) * n + (n - 1 - ref)]; break;
+        }
+      }
+      buf0[i * TWP + u] = v;
+    }
+  } else {
+    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * R_in * A_in * C;
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+      const int i = idx / TWP, u = idx % TWP;
+      const i64 ref = tbase + u - ap * i;
+      const i64 row = (r * ROWS + i) * A_in + ap;
+      T v = T(0);
+      if (ref >= 0 && ref < C) v = src[row * C + ref];
+      buf0[i * TWP + u] = v;
+    }
+  }
+  __syncthreads();
+
+  // ---- S stages in shared memory.
+  T *cur = buf0, *nxt = buf1;
+#pragma unroll
+  for (int j = 0; j < S; ++j) {
+    const int Al_in = 1 << j;
+    const int Rl_out = ROWS >> (j + 1);
+    const int Al_out = Al_in * 2;
+    for (int idx = threadIdx.x; idx < Rl_out * Al_out * TWP; idx += blockDim.x) {
+      const int u = idx % TWP;
+      const int row_out = idx / TWP;
+      const int m = row_out / Al_out, lo = row_out % Al_out;
+      const int li = lo >> 1, sh = li + (lo & 1);
+      const T e = cur[((2 * m) * Al_in + li) * TWP + u];
+      T v = e;
+      if (u >= sh) {
+        // Reference offset of the odd operand (member (2m+1)*2^j pre-shifted by a'*(2m+1)*2^j).
+        const i64 ref_odd = tbase + (u - sh) - ap * (i64)((2 * m + 1) << j);
+        if (ref_odd >= 0) v = add_rn(e, cur[((2 * m + 1) * Al_in + li) * TWP + (u - sh)]);
+      }
+      nxt[row_out * TWP + u] = v;
+    }
+    __syncthreads();
+    T *tmp = cur; cur = nxt; nxt = tmp;
+  }
+
+  // ---- store: local angle l is global angle a' * 2^S + l of row group r.
+  if (LAST) {
+    // out[b][q][c][a], angle innermost; here R_out == 1 and A_out == n.
+    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * C * n;
+    for (int idx = threadIdx.x; idx < kFwdW * ROWS; idx += blockDim.x) {
+      const int l = idx % ROWS, w = idx / ROWS;
+      const i64 c = c0 + w;
+      if (c < C) st_stream(&dst[c * n + ap * ROWS + l], cur[l * TWP + kFwdHalo + w]);
+    }
+  } else {
+    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * R_out * A_out * C;
+    for (int idx = threadIdx.x; idx < ROWS * kFwdW; idx += blockDim.x) {
+      const int l = idx / kFwdW, w = idx % kFwdW;
+      const i64 c = c0 + w;
+      if (c < C) dst[(r * A_out + ap * ROWS + l) * C + c] = cur[l * TWP + kFwdHalo + w];
+    }
+  }
+}
+
+// ---- host side --------------------------------------------------------------
+
+// Split L stages into passes of at most 5 stages, as even as possible.
+static int plan_passes(int L, int *sizes) {
+  if (L == 0) { sizes[0] = 0; return 1; }
+  const int P = (L + 4) / 5;
+  for (int p = 0; p < P; ++p) sizes[p] = L / P + (p < L % P ? 1 : 0);
+  return P;
+}
+
+template <typename T, int S, bool FIRST, bool LAST>
+static int launch_fwd_pass(const FwdPassArgs &a, cudaStream_t st) {
+  constexpr int ROWS = 1 << S;
+  const size_t smem = 2 * sizeof(T) * ROWS * (kFwdW + kFwdHalo);
+  auto kern = fwd_pass_kernel<T, S, FIRST, LAST>;
+  static bool configured = false;  // per-instantiation, host-side only
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  const i64 C = 2 * a.n - 1;
+  const i64 tiles = a.batch * 4 * (a.n >> S) * ((C + kFwdW - 1) / kFwdW);
+  kern<<<(unsigned)tiles, kFwdThreads, smem, st>>>(a);
+  return launch_status();
+}
+
+template <typename T, bool FIRST, bool LAST>
+static int dispatch_S(int S, const FwdPassArgs &a, cudaStream_t st) {
+  switch (S) {
+    case 0: return launch_fwd_pass<T, 0, FIRST, LAST>(a, st);
+    case 1: return launch_fwd_pass<T, 1, FIRST, LAST>(a, st);
+    case 2: return launch_fwd_pass<T, 2, FIRST, LAST>(a, st);
+    case 3: return launch_fwd_pass<T, 3, FIRST, LAST>(a, st);
+    case 4: return launch_fwd_pass<T, 4, FIRST, LAST>(a, st);
+    case 5: return launch_fwd_pass<T, 5, FIRST, LAST>(a, st);
+  }
+  return ADRT_GB300_ERR_SHAPE;
+}
+
+template <typename T>
+static int dispatch_pass(int S, bool first, bool last, const FwdPassArgs &a, cudaStream_t st) {
+  if (first && last) return dispatch_S<T, true, true>(S, a, st);
+  if (first) return dispatch_S<T, true, false>(S, a, st);
+  if (last) return dispatch_S<T, false, true>(S, a, st);
+  return dispatch_S<T, false, false>(S, a, st);
+}
+
+// Images per chunk: the intermediate of one chunk is meant to stay in L2.
+static i64 fwd_chunk(i64 batch, i64 n, size_t elem) {
+  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  const size_t budget = (size_t)48 << 20;
+  i64 k = (i64)(budget / per);
+  if (k < 1) k = 1;
+  return k < batch ? k : batch;
+}
+
+size_t fwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
+  int sizes[16];
+  const int P = plan_passes(num_iters(n), sizes);
+  if (P <= 1) return 0;
+  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  return per * (P >= 3 ? 2 : 1) * (size_t)fwd_chunk(batch, n, elem);
+}
+
+template <typename T>
+int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
+                 cudaStream_t st) {
+  int sizes[16];
+  const int P = plan_passes(num_iters(n), sizes);
+  const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
+  const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
+  i64 chunk = fwd_chunk(batch, n, sizeof(T));
+  if (nbuf) {
+    const i64 fit = (i64)(ws_bytes / (per * nbuf));
+    if (fit < 1 || ws == nullptr) return ADRT_GB300_ERR_WORKSPACE;
+    if (fit < chunk) chunk = fit;
+  }
+  T *bufs[2] = {static_cast<T *>(ws), nbuf == 2 ? reinterpret_cast<T *>(static_cast<char *>(ws) + per * chunk) : nullptr};
+  for (i64 b0 = 0; b0 < batch; b0 += chunk) {
+    const i64 nb = (batch - b0) < chunk ? (batch - b0) : chunk;
+    int k0 = 0;
+    const void *src = in + b0 * n * n;
+    for (int p = 0; p < P; ++p) {
+      const bool first = p == 0, last = p == P - 1;
+      void *dst = last ? static_cast<void *>(out + b0 * 4 * n * (2 * n - 1)) : bufs[p & 1];
+      FwdPassArgs a{src, dst, n, k0, nb};
+      int rc = dispatch_pass<T>(sizes[p], first, last, a, st);
+      if (rc) return rc;
+      k0 += sizes[p];
+      src = dst;
+    }
+  }
+  return ADRT_GB300_OK;
+}
+
+template int adrt_forward<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t);
+template int adrt_forward<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t);
+
+}  // namespace adrtg

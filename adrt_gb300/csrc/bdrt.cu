@@ -1,0 +1,245 @@
+// Backprojection (bdrt): the transpose of the forward butterfly, fused into
+// multi-stage passes.
+//
+// The reference runs log2(n) stages over a per-quadrant buffer [S][P][2n-1]
+// (S angles halving, P sections doubling, src/adrt/adrt_cdefs_bdrt.hpp:56-116):
+//   left   out[s][2p][c]       = in[2s][p][c] + in[2s+1][p][c]
+//   right  out[s][2p+1][c]     = in[2s][p][c+s] + in[2s+1][p][c+s+1]   (c+s+1 <= C-1)
+//          out[s][2p+1][C-1-s] = in[2s][p][C-1]                         (copy)
+//          out[s][2p+1][c]     = +0                                     (c >= C-s)
+// after transposing the (4, 2n-1, n) input to [n][1][2n-1] (:144-161) and
+// before transposing back (:170-185).
+//
+// bdrt stage j undoes forward stage L-1-j, so bdrt passes are forward passes
+// run backwards.  One CTA owns forward row group r at forward input angle a'
+// (i.e. bdrt angles a'*2^S + l, l < 2^S) and a window of W tile positions.
+// Member i of the pass output lives at tile position t <-> reference offset
+// t - a'*i, the same pre-shift as the forward pass, so inside the tile the
+// gathers are the small residual shifts l and l+1.  Loads are one window per
+// angle; stores go to a per-member shifted window.  Copy and zero rules are
+// evaluated on reference offsets, exactly as in the reference.
+#include "common.cuh"
+
+namespace adrtg {
+
+constexpr int kBwdW = 128;
+constexpr int kBwdHalo = 32;   // right halo (>= 2^S - 1)
+constexpr int kBwdThreads = 256;
+
+struct BwdPassArgs {
+  const void *in;  // final-layout array (first pass) or bdrt buffer
+  void *out;       // bdrt buffer, or final-layout output (last pass)
+  i64 n;
+  int k0;          // first forward stage covered by this pass
+  i64 batch;
+};
+
+// Buffer layout between passes, per (b, q): [angle s][section p][offset c],
+// the reference's bdrt buffer.  After forward stage k0 there are A = 2^k0
+// angles and R = n / 2^k0 sections.
+template <typename T, int S, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kBwdThreads)
+bwd_pass_kernel(BwdPassArgs args) {
+  constexpr int ROWS = 1 << S;
+  constexpr int TWP = kBwdW + kBwdHalo;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *buf0 = reinterpret_cast<T *>(smem_raw);
+  T *buf1 = buf0 + ROWS * TWP;
+
+  const i64 n = args.n;
+  const i64 C = 2 * n - 1;
+  const int k0 = args.k0;
+  const i64 A_lo = i64(1) << k0;   // angles after this pass (pass output)
+  const i64 R_lo = n >> k0;        // sections after this pass
+  const i64 A_hi = A_lo << S;      // angles at pass input
+  const i64 R_hi = R_lo >> S;      // sections at pass input
+  // Tile positions span [0, C + a'*(2^S-1)) so every member's window is covered.
+  const i64 max_ext = (A_lo - 1) * (ROWS - 1);
+  const int col_tiles = (int)((C + max_ext + kBwdW - 1) / kBwdW);
+
+  i64 t = blockIdx.x;
+  const int ct = (int)(t % col_tiles); t /= col_tiles;
+  const i64 ap = t % A_lo; t /= A_lo;
+  const i64 r = t % R_hi; t /= R_hi;
+  const int q = (int)(t % 4); t /= 4;
+  const i64 b = t;
+  const i64 c0 = (i64)ct * kBwdW;
+  // Skip tiles that hold no member's valid offsets.
+  if (c0 >= C + ap * (ROWS - 1)) return;
+
+  // ---- load angle l = a'*2^S + l of section r, tile positions [c0, c0+TWP).
+  if (FIRST) {
+    // in[b][q][c][angle], angle innermost; here R_hi == 1, A_hi == n.
+    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * C * n;
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+      const int l = idx % ROWS, u = idx / ROWS;
+      const i64 c = c0 + u;
+      T v = T(0);
+      if (c < C) v = src[c * n + ap * ROWS + l];
+      buf0[l * TWP + u] = v;
+    }
+  } else {
+    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * A_hi * R_hi * C;
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+      const int l = idx / TWP, u = idx % TWP;
+      const i64 c = c0 + u;
+      T v = T(0);
+      if (c < C) v = src[((ap * ROWS + l) * R_hi + r) * C + c];
+      buf0[l * TWP + u] = v;
+    }
+  }
+  __syncthreads();
+
+  // ---- S transposed stages, forward local stage j = S-1 down to 0.
+  // Level j+1 buffer rows: combo m, local angle la -> row m * 2^(j+1) + la.
+  // Level j buffer rows:   combo m', local angle li -> row m' * 2^j + li.
+  T *cur = buf0, *nxt = buf1;
+#pragma unroll
+  for (int j = S - 1; j >= 0; --j) {
+    const int Al_hi = 2 << j;          // local angles at level j+1
+    const int Al_lo = 1 << j;          // local angles at level j
+    const int Rl_lo = ROWS >> j;       // combos at level j
+    for (int idx = threadIdx.x; idx < Rl_lo * Al_lo * TWP; idx += blockDim.x) {
+      const int u = idx % TWP;
+      const int row = idx / TWP;
+      const int mm = row / Al_lo, li = row % Al_lo;  // level-j combo, angle
+      const int m = mm >> 1;                         // parent combo at level j+1
+      const T *ya = cur + (m * Al_hi + 2 * li) * TWP;
+      const T *yb = ya + TWP;
+      T v;
+      if ((mm & 1) == 0) {
+        v = add_rn(ya[u], yb[u]);  // left (garbage beyond the buffer is never used)
+      } else {
+        // Reference offset of ya's operand: tile position u+li, parent mapping a'*2m*2^j.
+        const i64 ref_la = c0 + u + li - ap * (i64)((2 * m) << j);
+        if (u + li + 1 < TWP && ref_la + 1 <= C - 1) v = add_rn(ya[u + li], yb[u + li + 1]);
+        else if (ref_la == C - 1 && u + li < TWP) v = ya[u + li];
+        else v = T(0);
+      }
+      nxt[row * TWP + u] = v;
+    }
+    __syncthreads();
+    T *tmp = cur; cur = nxt; nxt = tmp;
+  }
+
+  // ---- store member i (section r*2^S + i at angle a') at reference offset u + c0 - a'*i.
+  if (LAST) {
+    // out[b][q][c][section], section innermost; A_lo == 1, a' == 0.
+    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * C * n;
+    for (int idx = threadIdx.x; idx < kBwdW * ROWS; idx += blockDim.x) {
+      const int i = idx % ROWS, w = idx / ROWS;
+      const i64 c = c0 + w;
+      if (c < C) st_stream(&dst[c * n + r * ROWS + i], cur[i * TWP + w]);
+    }
+  } else {
+    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * A_lo * R_lo * C;
+    for (int idx = threadIdx.x; idx < ROWS * kBwdW; idx += blockDim.x) {
+      const int i = idx / kBwdW, w = idx % kBwdW;
+      const i64 c = c0 + w - ap * i;
+      if (c >= 0 && c < C) dst[(ap * R_lo + r * ROWS + i) * C + c] = cur[i * TWP + w];
+    }
+  }
+}
+
+static int plan_passes_bwd(int L, int *sizes) {
+  if (L == 0) { sizes[0] = 0; return 1; }
+  const int P = (L + 4) / 5;
+  for (int p = 0; p < P; ++p) sizes[p] = L / P + (p < L % P ? 1 : 0);
+  return P;
+}
+
+template <typename T, int S, bool FIRST, bool LAST>
+static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
+  constexpr int ROWS = 1 << S;
+  const size_t smem = 2 * sizeof(T) * ROWS * (kBwdW + kBwdHalo);
+  auto kern = bwd_pass_kernel<T, S, FIRST, LAST>;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  const i64 C = 2 * a.n - 1;
+  const i64 A_lo = i64(1) << a.k0;
+  const i64 max_ext = (A_lo - 1) * (ROWS - 1);
+  const i64 col_tiles = (C + max_ext + kBwdW - 1) / kBwdW;
+  const i64 tiles = a.batch * 4 * ((a.n >> a.k0) >> S) * A_lo * col_tiles;
+  kern<<<(unsigned)tiles, kBwdThreads, smem, st>>>(a);
+  return launch_status();
+}
+
+template <typename T, bool FIRST, bool LAST>
+static int bwd_dispatch_S(int S, const BwdPassArgs &a, cudaStream_t st) {
+  switch (S) {
+    case 0: return launch_bwd_pass<T, 0, FIRST, LAST>(a, st);
+    case 1: return launch_bwd_pass<T, 1, FIRST, LAST>(a, st);
+    case 2: return launch_bwd_pass<T, 2, FIRST, LAST>(a, st);
+    case 3: return launch_bwd_pass<T, 3, FIRST, LAST>(a, st);
+    case 4: return launch_bwd_pass<T, 4, FIRST, LAST>(a, st);
+    case 5: return launch_bwd_pass<T, 5, FIRST, LAST>(a, st);
+  }
+  return ADRT_GB300_ERR_SHAPE;
+}
+
+template <typename T>
+static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cudaStream_t st) {
+  if (first && last) return bwd_dispatch_S<T, true, true>(S, a, st);
+  if (first) return bwd_dispatch_S<T, true, false>(S, a, st);
+  if (last) return bwd_dispatch_S<T, false, true>(S, a, st);
+  return bwd_dispatch_S<T, false, false>(S, a, st);
+}
+
+static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
+  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  const size_t budget = (size_t)48 << 20;
+  i64 k = (i64)(budget / per);
+  if (k < 1) k = 1;
+  return k < batch ? k : batch;
+}
+
+size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
+  int sizes[16];
+  const int P = plan_passes_bwd(num_iters(n), sizes);
+  if (P <= 1) return 0;
+  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  return per * (P >= 3 ? 2 : 1) * (size_t)bwd_chunk(batch, n, elem);
+}
+
+template <typename T>
+int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
+                 cudaStream_t st) {
+  int sizes[16];
+  const int P = plan_passes_bwd(num_iters(n), sizes);
+  const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
+  const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
+  i64 chunk = bwd_chunk(batch, n, sizeof(T));
+  if (nbuf) {
+    const i64 fit = (i64)(ws_bytes / (per * nbuf));
+    if (fit < 1 || ws == nullptr) return ADRT_GB300_ERR_WORKSPACE;
+    if (fit < chunk) chunk = fit;
+  }
+  T *bufs[2] = {static_cast<T *>(ws),
+                nbuf == 2 ? reinterpret_cast<T *>(static_cast<char *>(ws) + per * chunk) : nullptr};
+  // Forward pass p covers stages [k_p, k_p + sizes[p]); run them last to first.
+  int kstart[16];
+  int k = 0;
+  for (int p = 0; p < P; ++p) { kstart[p] = k; k += sizes[p]; }
+  for (i64 b0 = 0; b0 < batch; b0 += chunk) {
+    const i64 nb = (batch - b0) < chunk ? (batch - b0) : chunk;
+    const void *src = in + b0 * 4 * n * (2 * n - 1);
+    for (int s = 0; s < P; ++s) {
+      const int p = P - 1 - s;
+      const bool first = s == 0, last = s == P - 1;
+      void *dst = last ? static_cast<void *>(out + b0 * 4 * n * (2 * n - 1)) : bufs[s & 1];
+      BwdPassArgs a{src, dst, n, kstart[p], nb};
+      int rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
+      if (rc) return rc;
+      src = dst;
+    }
+  }
+  return ADRT_GB300_OK;
+}
+
+template int bdrt_forward<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t);
+template int bdrt_forward<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t);
+
+}  // namespace adrtg

@@ -1,0 +1,64 @@
+// Shared definitions for the adrt_gb300 CUDA library.
+//
+// Numerics: every kernel computes each output with the same operand pairing,
+// operand order and copy-versus-add rule as the reference routine it replaces,
+// so results are bit-identical.  The library is compiled with -fmad=false and
+// without fast-math; adds that must not be reordered use __fadd_rn/__dadd_rn.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/adrt_gb300.h"
+
+namespace adrtg {
+
+using i64 = long long;
+
+// ---- exact arithmetic helpers --------------------------------------------
+
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+// ---- cache-hinted global access -------------------------------------------
+
+// Streaming store for final outputs: written once, never re-read by us.
+template <typename T>
+__device__ __forceinline__ void st_stream(T *p, T v) { __stcs(p, v); }
+
+// ---- host-side helpers ----------------------------------------------------
+
+inline int num_iters(i64 n) {
+  if (n <= 1) return 0;
+  int bits = 0;
+  for (i64 v = n; v; v >>= 1) ++bits;
+  return bits - (((n & (n - 1)) == 0) ? 1 : 0);
+}
+
+inline bool is_pow2(i64 n) { return n > 0 && (n & (n - 1)) == 0; }
+
+inline size_t dtype_size(int dtype) {
+  return dtype == ADRT_GB300_F32 ? 4 : (dtype == ADRT_GB300_F64 ? 8 : 0);
+}
+
+inline int ceil_div_i(i64 a, i64 b) { return (int)((a + b - 1) / b); }
+
+// Count of kernel launches enqueued by this library (reported through
+// adrt_gb300_launch_count); defined in capi.cu.
+void count_launch();
+
+// Map a CUDA error from a launch to the library status; every kernel launch
+// in the library is followed by exactly one call.
+inline int launch_status() {
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ADRT_GB300_OK : ADRT_GB300_ERR_CUDA;
+}
+
+}  // namespace adrtg

@@ -1,0 +1,105 @@
+// Exact inverse ADRT.
+//
+// The reference (src/adrt/adrt_cdefs_iadrt.hpp:53-105) runs log2(n) stages; in
+// stage s every chain (l, col), l < 2^(s+1), col < n / 2^(s+1), is a serial
+// recurrence from the last offset row down to row 0:
+//   l even: v = (0 + E[row]) - O[row+1]             (O term if row+1 < R)
+//   l odd:  v = (0 + O[row+1+col]) - E[row+1+col]   (if row+1+col < R, else 0)
+//   v += out[row+1]                                  (if row+1 < R)
+// with E, O the input chains (l/2, 2col) and (l/2, 2col+1), R = 2n-1.
+//
+// The recurrence is kept serial per chain (same operation order, so the
+// ill-conditioned result is bit-identical).  The GPU layout is
+// [row][chain] per (batch, quadrant), chain = l * (n/2^(s+1)) + col, so that a
+// warp's chains are adjacent in memory at every row; the reference's input
+// (4, 2n-1, n) is already this layout with chain = angle, and so is its output.
+#include "common.cuh"
+
+namespace adrtg {
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i64 n, int s) {
+  const i64 R = 2 * n - 1;
+  const i64 Cc = n >> s;           // input chains per l
+  const i64 C2 = Cc >> 1;          // output chains per l
+  const i64 chains = n;            // per plane, at every stage
+  const i64 gid = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  if (gid >= planes * chains) return;
+  const i64 plane = gid / chains;
+  const i64 ch = gid % chains;
+  const i64 l = ch / C2, col = ch % C2;
+  const i64 pl = l >> 1;
+  const T *src = in + plane * R * n;
+  T *dst = out + plane * R * n;
+  const i64 e_ch = pl * Cc + 2 * col;
+  const i64 o_ch = e_ch + 1;
+  T prev = T(0);
+  if ((l & 1) == 0) {
+    for (i64 row = R - 1; row >= 0; --row) {
+      T v = add_rn(T(0), src[row * n + e_ch]);
+      if (row + 1 < R) {
+        v = sub_rn(v, src[(row + 1) * n + o_ch]);
+        v = add_rn(v, prev);
+      }
+      dst[row * n + ch] = v;
+      prev = v;
+    }
+  } else {
+    const i64 d = 1 + col;
+    for (i64 row = R - 1; row >= 0; --row) {
+      T v = T(0);
+      if (row + d < R) {
+        v = add_rn(v, src[(row + d) * n + o_ch]);
+        v = sub_rn(v, src[(row + d) * n + e_ch]);
+      }
+      if (row + 1 < R) v = add_rn(v, prev);
+      dst[row * n + ch] = v;
+      prev = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void copy_kernel(const T *__restrict__ in, T *__restrict__ out, i64 total) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < total;
+       i += (i64)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+size_t iadrt_workspace_bytes(i64 batch, i64 n, size_t elem) {
+  const int L = num_iters(n);
+  const size_t per = (size_t)batch * 4 * n * (2 * n - 1) * elem;
+  return L >= 3 ? 2 * per : (L == 2 ? per : 0);
+}
+
+template <typename T>
+int iadrt_launch(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
+                 cudaStream_t st) {
+  const int L = num_iters(n);
+  const i64 planes = batch * 4;
+  const i64 elems = planes * n * (2 * n - 1);
+  if (L == 0) {
+    copy_kernel<T><<<(unsigned)((elems + 255) / 256), 256, 0, st>>>(in, out, elems);
+    return launch_status();
+  }
+  if (ws_bytes < iadrt_workspace_bytes(batch, n, sizeof(T)) || (L >= 2 && ws == nullptr))
+    return ADRT_GB300_ERR_WORKSPACE;
+  T *bufs[2] = {static_cast<T *>(ws), static_cast<T *>(ws) + elems};
+  const T *src = in;
+  const i64 threads = planes * n;
+  const unsigned grid = (unsigned)((threads + 127) / 128);
+  for (int s = 0; s < L; ++s) {
+    T *dst = (s == L - 1) ? out : bufs[s & 1];
+    iadrt_stage_kernel<T><<<grid, 128, 0, st>>>(src, dst, planes, n, s);
+    const int rc = launch_status();
+    if (rc) return rc;
+    src = dst;
+  }
+  return ADRT_GB300_OK;
+}
+
+template int iadrt_launch<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t);
+template int iadrt_launch<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t);
+
+}  // namespace adrtg

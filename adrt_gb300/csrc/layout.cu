@@ -1,0 +1,157 @@
+// Layout kernels: adrt_init, truncate, stitch (pure copies, any element size)
+// and the quadrant sum of the adjoint.
+#include "common.cuh"
+
+namespace adrtg {
+
+// Element-size-generic storage types (copies only move bits).
+template <int B> struct word;
+template <> struct word<1> { using t = uint8_t; };
+template <> struct word<2> { using t = uint16_t; };
+template <> struct word<4> { using t = uint32_t; };
+template <> struct word<8> { using t = uint64_t; };
+struct alignas(16) w16 {
+  uint64_t lo, hi;
+  w16() = default;
+  __host__ __device__ explicit w16(int) : lo(0), hi(0) {}
+};
+template <> struct word<16> { using t = w16; };
+
+// (n, n) image -> (4, 2n-1, n):  q0[c][a] = x[a][n-1-c], q1[c][a] = x[n-1-c][a],
+// q2[c][a] = x[c][a], q3[c][a] = x[n-1-a][n-1-c]; zero for c >= n.
+// Reference: src/adrt/core.py:170-175.
+template <typename W>
+__global__ void init_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n) {
+  const i64 C = 2 * n - 1;
+  const i64 total = batch * 4 * C * n;
+  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
+       idx += (i64)gridDim.x * blockDim.x) {
+    const i64 a = idx % n;
+    const i64 c = (idx / n) % C;
+    const int q = (int)((idx / (n * C)) % 4);
+    const i64 b = idx / (4 * n * C);
+    const W *x = in + b * n * n;
+    W v = W(0);
+    if (c < n) {
+      switch (q) {
+        case 0: v = x[a * n + (n - 1 - c)]; break;
+        case 1: v = x[(n - 1 - c) * n + a]; break;
+        case 2: v = x[c * n + a]; break;
+        default: v = x[(n - 1 - a) * n + (n - 1 - c)]; break;
+      }
+    }
+    out[idx] = v;
+  }
+}
+
+// Index into quadrant q of an ADRT array for truncate's output (i, j).
+// Reference: src/adrt/utils.py:234-242.
+__device__ __forceinline__ i64 trunc_src(int q, i64 i, i64 j, i64 n) {
+  switch (q) {
+    case 0: return (n - 1 - j) * n + i;
+    case 1: return (n - 1 - i) * n + j;
+    case 2: return i * n + j;
+    default: return (n - 1 - j) * n + (n - 1 - i);
+  }
+}
+
+template <typename W>
+__global__ void truncate_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n) {
+  const i64 C = 2 * n - 1;
+  const i64 total = batch * 4 * n * n;
+  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
+       idx += (i64)gridDim.x * blockDim.x) {
+    const i64 j = idx % n;
+    const i64 i = (idx / n) % n;
+    const i64 bq = idx / (n * n);
+    out[idx] = in[bq * C * n + trunc_src((int)(bq % 4), i, j, n)];
+  }
+}
+
+// (4, 2n-1, n) -> (3n-2, 4, vc): quadrant k flipped on both axes when k is
+// odd, last column dropped when remove_repeated, rows offset by n-1 for k >= 2.
+// Reference: src/adrt/utils.py:111-134.
+template <typename W>
+__global__ void stitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n,
+                              int remove_repeated) {
+  const i64 C = 2 * n - 1, OR = 3 * n - 2;
+  const i64 vc = n - (remove_repeated ? 1 : 0);
+  const i64 total = batch * OR * 4 * vc;
+  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
+       idx += (i64)gridDim.x * blockDim.x) {
+    const i64 col = idx % vc;
+    const int k = (int)((idx / vc) % 4);
+    const i64 row = (idx / (4 * vc)) % OR;
+    const i64 b = idx / (4 * vc * OR);
+    const i64 rr = row - (k >= 2 ? n - 1 : 0);
+    W v = W(0);
+    if (rr >= 0 && rr < C) {
+      const i64 sr = (k & 1) ? C - 1 - rr : rr;
+      const i64 sc = (k & 1) ? n - 1 - col : col;
+      v = in[((b * 4 + k) * C + sr) * n + sc];
+    }
+    out[idx] = v;
+  }
+}
+
+// Adjoint tail: out[b][i][j] = ((t0 + t1) + t2) + t3 with t_q = truncate(y)[q].
+template <typename T>
+__global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, i64 batch, i64 n) {
+  const i64 C = 2 * n - 1;
+  const i64 total = batch * n * n;
+  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
+       idx += (i64)gridDim.x * blockDim.x) {
+    const i64 j = idx % n;
+    const i64 i = (idx / n) % n;
+    const T *yb = y + (idx / (n * n)) * 4 * C * n;
+    T s = add_rn(yb[trunc_src(0, i, j, n)], yb[C * n + trunc_src(1, i, j, n)]);
+    s = add_rn(s, yb[2 * C * n + trunc_src(2, i, j, n)]);
+    out[idx] = add_rn(s, yb[3 * C * n + trunc_src(3, i, j, n)]);
+  }
+}
+
+static unsigned grid_l(i64 total) {
+  i64 g = (total + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+#define BY_SIZE(ES, KERNEL, TOTAL, ...)                                                     \
+  switch (ES) {                                                                             \
+    case 1: KERNEL<word<1>::t><<<grid_l(TOTAL), 256, 0, st>>>(                              \
+        (const word<1>::t *)in, (word<1>::t *)out, __VA_ARGS__); break;                     \
+    case 2: KERNEL<word<2>::t><<<grid_l(TOTAL), 256, 0, st>>>(                              \
+        (const word<2>::t *)in, (word<2>::t *)out, __VA_ARGS__); break;                     \
+    case 4: KERNEL<word<4>::t><<<grid_l(TOTAL), 256, 0, st>>>(                              \
+        (const word<4>::t *)in, (word<4>::t *)out, __VA_ARGS__); break;                     \
+    case 8: KERNEL<word<8>::t><<<grid_l(TOTAL), 256, 0, st>>>(                              \
+        (const word<8>::t *)in, (word<8>::t *)out, __VA_ARGS__); break;                     \
+    case 16: KERNEL<word<16>::t><<<grid_l(TOTAL), 256, 0, st>>>(                            \
+        (const word<16>::t *)in, (word<16>::t *)out, __VA_ARGS__); break;                   \
+    default: return ADRT_GB300_ERR_DTYPE;                                                   \
+  }
+
+int init_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cudaStream_t st) {
+  BY_SIZE(es, init_kernel, batch * 4 * (2 * n - 1) * n, batch, n)
+  return launch_status();
+}
+
+int truncate_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cudaStream_t st) {
+  BY_SIZE(es, truncate_kernel, batch * 4 * n * n, batch, n)
+  return launch_status();
+}
+
+int stitch_launch(const void *in, void *out, i64 batch, i64 n, int rr, size_t es, cudaStream_t st) {
+  BY_SIZE(es, stitch_kernel, batch * (3 * n - 2) * 4 * n, batch, n, rr)
+  return launch_status();
+}
+
+template <typename T>
+int quad_sum_launch(const T *y, T *out, i64 batch, i64 n, cudaStream_t st) {
+  quad_sum_kernel<T><<<grid_l(batch * n * n), 256, 0, st>>>(y, out, batch, n);
+  return launch_status();
+}
+template int quad_sum_launch<float>(const float *, float *, i64, i64, cudaStream_t);
+template int quad_sum_launch<double>(const double *, double *, i64, i64, cudaStream_t);
+
+}  // namespace adrtg

@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark of the ADRT hot path on GB300.
+
+Workload: batched forward ADRT of 256 images of 1024 x 1024 float32 (half
+uniform [0, 1), half random-ellipse phantoms), the batched configuration the
+headline metric is quoted on.  One step = one forward ADRT of the whole
+batch.  Inputs (1 GiB) and outputs (8.6 GB) are far larger than L2, so no L2
+flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line on rank 0.  Under torchrun (N > 1) every rank runs its
+own batch of 256 images (weak scaling, no collective on the data path); the
+time is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ADRT img/s N=1024 fp32 (%HBM roofline); CG solves/s @1e-4, learned vs plain"
+UNIT = "img/s"
+WORKLOAD = "adrt_forward_batched_256x1024x1024_f32"
+
+
+def bytes_per_image(n: int, elem: int) -> int:
+    """Compulsory traffic of one forward ADRT: read the image once, write the
+    (4, 2n-1, n) output once."""
+    return elem * (n * n + 4 * n * (2 * n - 1))
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(workload: str):
+    """DRAM bytes per image from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(workload)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sms.append(float(parts[0]))
+                maxes.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxes),
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def gpu_uuid(torch, dev) -> str:
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return str(dev)
+
+
+def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
+    """Times the CPU restatement (all host threads) on a bounded sample."""
+    import numpy as np
+
+    from oracle import oracle
+
+    kind = "port"
+    fn = oracle.adrt
+    try:
+        from oracle import ref
+
+        A = ref.load()
+        if A is not None:
+            fn, kind = A.adrt, "reference"
+    except Exception:
+        pass
+    x = np.random.default_rng(0).random((batch, n, n), dtype=np.float32).astype(dtype)
+    fn(x[:1])  # warm
+    t0 = time.perf_counter()
+    imgs = 0
+    while True:
+        fn(x)
+        imgs += batch
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return {
+        "value": imgs / el,
+        "unit": UNIT,
+        "cores": oracle.threads(),
+        "kind": kind,
+        "sample": f"{imgs} images of {n}x{n} {dtype} in batches of {batch} ({el:.1f} s)",
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle import oracle
+
+    kind = "port"
+    fn = oracle.adrt
+    try:
+        from oracle import ref
+
+        A = ref.load()
+        if A is not None:
+            fn, kind = A.adrt, "reference"
+    except Exception:
+        pass
+    sample = 8
+    x = np.random.default_rng(0).random((sample, args.n, args.n), dtype=np.float32)
+    for _ in range(args.warmup):
+        fn(x)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn(x)
+    el = time.perf_counter() - t0
+    value = sample * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_images_per_step": sample, "n": args.n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(), "kind": kind,
+                         "sample": f"{sample} images of {args.n}x{args.n} float32 per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import adrt_gb300 as adrt
+    from adrt_gb300 import _lib
+    from adrt_gb300.data import mixed_batch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v: float) -> float:
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    n, B = args.n, args.batch
+    x = mixed_batch(B, n, seed=1000 * rank, device=dev, dtype=torch.float32)
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput --------------------------------------
+    for _ in range(args.warmup):
+        y = adrt.adrt(x)
+    del y
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_uuid(torch, dev)) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        y = adrt.adrt(x)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - launches0
+    barrier()
+    clocks = sampler.stop() if sampler else None
+    t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
+    value = world * B * args.steps / t_dev
+    del y
+
+    # ---- end to end through host buffers ----------------------------------
+    xh = x.cpu().pin_memory()
+    for _ in range(1):
+        yh = adrt.adrt(xh)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        yh = adrt.adrt(xh)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    e2e = {
+        "value": world * B * args.e2e_steps / t_e2e,
+        "unit": UNIT,
+        "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
+        "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
+    }
+    del yh
+
+    extras = {}
+    if not args.no_extras:
+        yd = adrt.adrt(x)
+        for _ in range(3):
+            z = adrt.bdrt(yd)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ks = max(3, args.steps // 3)
+        for _ in range(ks):
+            z = adrt.bdrt(yd)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        extras["bdrt_img_s"] = B * ks / (e0.elapsed_time(e1) / 1000.0)
+        del z, yd
+        x64 = x[:64].double()
+        for _ in range(3):
+            y64 = adrt.adrt(x64)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(ks):
+            y64 = adrt.adrt(x64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1) / 1000.0
+        extras["adrt_f64_img_s"] = 64 * ks / t64
+        extras["adrt_f64_gbs"] = 64 * ks * bytes_per_image(n, 8) / t64 / 1e9
+        del y64, x64
+
+    peak, peak_src = load_peaks()
+    bpi = bytes_per_image(n, 4)
+    achieved = value / world * bpi / 1e9
+    traffic = load_traffic(WORKLOAD)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_dev / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD,
+            "batch_per_gpu": B,
+            "n": n,
+            "inputs": "half uniform [0,1), half random-ellipse phantoms",
+            "l2": "inputs and outputs larger than L2 (no flush)",
+            "parallelism": f"batch sharding x{world}" if world > 1 else "single GPU",
+        },
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_source": peak_src,
+            "kernel": "adrt forward (fused passes), op-level: compulsory bytes per image x img/s",
+            "bytes_per_image": bpi,
+        },
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    line.update(extras)
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline_run(n, "float32", args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

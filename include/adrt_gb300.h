@@ -1,0 +1,172 @@
+/*
+ * adrt_gb300.h -- C ABI of the GB300 (sm_103a) ADRT library.
+ *
+ * Every entry point takes device pointers to C-contiguous arrays, plain sizes,
+ * a dtype code and a CUDA stream (passed as void*, i.e. a cudaStream_t; NULL
+ * is the legacy default stream).  Work is enqueued on that stream; the call
+ * returns once it is enqueued.  No entry point allocates device memory: ops
+ * that need a temporary take a caller-provided workspace whose size is given
+ * by adrt_gb300_workspace_size().  Nothing throws across this boundary; each
+ * call returns an adrt_gb300 status code.
+ *
+ * Shapes follow the reference package (karlotness/adrt):
+ *   image      (batch, n, n)              n a power of two
+ *   ADRT array (batch, 4, 2n-1, n)        quadrant, offset, angle
+ * with a batch of 1 standing for the reference's unbatched arrays.
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * the reference repository).  In the reference those routines are reached
+ * through the CPython module adrt._adrt_cdefs (src/adrt/adrt_cdefs_py.cpp:852-909),
+ * whose argument checks and error messages the Python package adrt_gb300
+ * reproduces before calling in here.
+ */
+#ifndef ADRT_GB300_H
+#define ADRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  ADRT_GB300_OK = 0,
+  ADRT_GB300_ERR_SHAPE = 1,     /* shape not valid for the op (reference: ValueError) */
+  ADRT_GB300_ERR_STEP = 2,      /* step out of range (reference: ValueError) */
+  ADRT_GB300_ERR_DTYPE = 3,     /* dtype not float32/float64 (reference: TypeError) */
+  ADRT_GB300_ERR_WORKSPACE = 4, /* workspace missing or smaller than required */
+  ADRT_GB300_ERR_NULL = 5,      /* a required pointer is NULL */
+  ADRT_GB300_ERR_CUDA = 6,      /* the CUDA runtime reported an error */
+  ADRT_GB300_ERR_TIMEOUT = 7,   /* a bounded device-side wait expired */
+  ADRT_GB300_ERR_TOO_LARGE = 8  /* size arithmetic overflows (reference: ValueError) */
+};
+
+/* Dtype codes. */
+enum { ADRT_GB300_F32 = 0, ADRT_GB300_F64 = 1 };
+
+/* Ops that take a workspace. */
+enum {
+  ADRT_GB300_OP_ADRT = 0,
+  ADRT_GB300_OP_BDRT = 1,
+  ADRT_GB300_OP_IADRT = 2,
+  ADRT_GB300_OP_ADJOINT = 3
+};
+
+/* Human-readable text for a status code (static storage). */
+const char *adrt_gb300_status_string(int status);
+
+/* ceil(log2(n)), 0 for n <= 1.
+ * Replaces adrt::num_iters (src/adrt/adrt_cdefs_common.cpp:140-142). */
+int adrt_gb300_num_iters(int64_t n);
+
+/* Number of CUDA kernel launches this library has enqueued since it was
+ * loaded (all threads, all devices).  For accounting; no reference counterpart. */
+uint64_t adrt_gb300_launch_count(void);
+
+/* Bytes of workspace that `op` needs for `batch` arrays of side n.  May be 0.
+ * The reference allocates this temporary itself with PyMem_Malloc
+ * (src/adrt/adrt_cdefs_py.cpp:301-307). */
+int adrt_gb300_workspace_size(int op, int64_t batch, int64_t n, int dtype, size_t *bytes);
+
+/* Forward ADRT: in (batch, n, n) -> out (batch, 4, 2n-1, n).
+ * Replaces adrt::adrt_basic (src/adrt/adrt_cdefs_adrt.hpp:101-212),
+ * bound as _adrt_cdefs.adrt (src/adrt/adrt_cdefs_py.cpp:275-341). */
+int adrt_gb300_adrt(const void *in, void *out, int64_t batch, int64_t n, int dtype,
+                    void *workspace, size_t workspace_bytes, void *stream);
+
+/* One forward stage in the output layout: (batch, 4, 2n-1, n) -> same.
+ * Replaces adrt::adrt_step (src/adrt/adrt_cdefs_adrt.hpp:215-258),
+ * bound as _adrt_cdefs.adrt_step (src/adrt/adrt_cdefs_py.cpp:343-412). */
+int adrt_gb300_adrt_step(const void *in, void *out, int64_t batch, int64_t n, int step,
+                         int dtype, void *stream);
+
+/* Backprojection: (batch, 4, 2n-1, n) -> same.
+ * Replaces adrt::bdrt_basic (src/adrt/adrt_cdefs_bdrt.hpp:121-187),
+ * bound as _adrt_cdefs.bdrt (src/adrt/adrt_cdefs_py.cpp:482-548). */
+int adrt_gb300_bdrt(const void *in, void *out, int64_t batch, int64_t n, int dtype,
+                    void *workspace, size_t workspace_bytes, void *stream);
+
+/* One backprojection stage: (batch, 4, 2n-1, n) -> same.
+ * Replaces adrt::bdrt_step (src/adrt/adrt_cdefs_bdrt.hpp:190-244),
+ * bound as _adrt_cdefs.bdrt_step (src/adrt/adrt_cdefs_py.cpp:550-619). */
+int adrt_gb300_bdrt_step(const void *in, void *out, int64_t batch, int64_t n, int step,
+                         int dtype, void *stream);
+
+/* Exact inverse: (batch, 4, 2n-1, n) -> same.
+ * Replaces adrt::iadrt_basic (src/adrt/adrt_cdefs_iadrt.hpp:110-176),
+ * bound as _adrt_cdefs.iadrt (src/adrt/adrt_cdefs_py.cpp:414-480). */
+int adrt_gb300_iadrt(const void *in, void *out, int64_t batch, int64_t n, int dtype,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* Transpose of the forward ADRT: (batch, 4, 2n-1, n) -> (batch, n, n), equal
+ * to truncate(bdrt(a)) summed over quadrants in order ((q0+q1)+q2)+q3.
+ * Replaces the user-level composition documented at src/adrt/_wrappers.py:283-284
+ * (exactness test: tests/test_bdrt.py:310-325). */
+int adrt_gb300_adjoint(const void *in, void *out, int64_t batch, int64_t n, int dtype,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* Quadrant initialisation: image (batch, n, n) -> (batch, 4, 2n-1, n), zeros
+ * below the top n rows.  Any element type (elem_size 1, 2, 4 or 8 bytes).
+ * Replaces adrt.core.adrt_init (src/adrt/core.py:123-176). */
+int adrt_gb300_adrt_init(const void *in, void *out, int64_t batch, int64_t n,
+                         size_t elem_size, void *stream);
+
+/* Truncate: (batch, 4, 2n-1, n) -> (batch, 4, n, n), each quadrant un-rotated.
+ * Any element type.  Replaces adrt.utils.truncate (src/adrt/utils.py:191-242). */
+int adrt_gb300_truncate(const void *in, void *out, int64_t batch, int64_t n,
+                        size_t elem_size, void *stream);
+
+/* Stitch: (batch, 4, 2n-1, n) -> (batch, 3n-2, 4*(n - remove_repeated)).
+ * Any element type.  Replaces adrt.utils.stitch_adrt (src/adrt/utils.py:65-134). */
+int adrt_gb300_stitch(const void *in, void *out, int64_t batch, int64_t n,
+                      int remove_repeated, size_t elem_size, void *stream);
+
+/* Multigrid restriction: (batch, 4, 2n-1, n) -> (batch, 4, n-1, n/2), n even.
+ * Replaces adrt::fmg_restriction (src/adrt/adrt_cdefs_fmg.hpp:53-73),
+ * bound as _adrt_cdefs.press_fmg_restriction (src/adrt/adrt_cdefs_py.cpp:684-738). */
+int adrt_gb300_fmg_restriction(const void *in, void *out, int64_t batch, int64_t n,
+                               int dtype, void *stream);
+
+/* Multigrid prolongation: (batch, h, w) -> (batch, 2h, 2w).
+ * Replaces adrt::fmg_prolongation (src/adrt/adrt_cdefs_fmg.hpp:75-95),
+ * bound as _adrt_cdefs.press_fmg_prolongation (src/adrt/adrt_cdefs_py.cpp:740-794). */
+int adrt_gb300_fmg_prolongation(const void *in, void *out, int64_t batch, int64_t h,
+                                int64_t w, int dtype, void *stream);
+
+/* Multigrid high-pass filter: (batch, h, w) -> same, h, w >= 2.
+ * Replaces adrt::fmg_highpass (src/adrt/adrt_cdefs_fmg.hpp:97-171),
+ * bound as _adrt_cdefs.press_fmg_highpass (src/adrt/adrt_cdefs_py.cpp:796-850). */
+int adrt_gb300_fmg_highpass(const void *in, void *out, int64_t batch, int64_t h,
+                            int64_t w, int dtype, void *stream);
+
+/* ---- Full-multigrid glue.  The reference evaluates these steps with NumPy
+ * inside adrt.core.iadrt_fmg_step / iadrt_fmg_iter / adrt.iadrt_fmg; these
+ * entry points compute the same values on the device. ------------------ */
+
+/* out (batch, n, n) = mean over quadrants of truncate(y) / (n - 1), for
+ * y (batch, 4, 2n-1, n): each term divided by (n-1), summed in quadrant order,
+ * then divided by 4.  Replaces the NumPy expression at src/adrt/core.py:328-329. */
+int adrt_gb300_fmg_correction(const void *y, void *out, int64_t batch, int64_t n, int dtype,
+                              void *stream);
+
+/* Elementwise out = a - b (op 0) or a + b (op 1) over `count` elements; out
+ * may alias a.  Replaces the NumPy array arithmetic at src/adrt/core.py:327-330
+ * and src/adrt/core.py:378. */
+int adrt_gb300_elementwise(int op, const void *a, const void *b, void *out, int64_t count,
+                           int dtype, void *stream);
+
+/* Sum of squares of `count` elements accumulated in float64 with a fixed
+ * (deterministic) order, written to the device double *out.  workspace must
+ * hold adrt_gb300_sumsq_workspace_size() bytes.  Used for the residual norm
+ * of the stopping rule at src/adrt/__init__.py:131-146. */
+size_t adrt_gb300_sumsq_workspace_size(void);
+int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void *workspace,
+                     void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADRT_GB300_H */

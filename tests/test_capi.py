@@ -1,0 +1,101 @@
+"""The C ABI library loads and exports every symbol its header declares; its
+argument checks return the documented status codes.  No GPU work is issued:
+every call here fails validation before touching the device."""
+
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        names |= set(re.findall(r"\b(adrt_gb300_\w+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from adrt_gb300 import _lib
+
+    if not os.path.exists(_lib.LIB_PATH):
+        from adrt_gb300 import build
+
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "adrt_gb300_adrt" in names and "adrt_gb300_bdrt" in names
+    assert len(names) >= 15
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header():
+    from adrt_gb300 import _lib
+
+    assert set(_declared()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings(lib):
+    from adrt_gb300 import _lib
+
+    for code in range(9):
+        s = _lib.status_string(code)
+        assert s and s != "unknown status"
+    assert _lib.status_string(99) == "unknown status"
+
+
+def test_num_iters(lib):
+    for n, want in [(0, 0), (1, 0), (2, 1), (3, 2), (1024, 10), (2**40 + 1, 41)]:
+        assert lib.adrt_gb300_num_iters(n) == want
+
+
+def test_validation_codes(lib):
+    from adrt_gb300 import _lib
+
+    fake = ctypes.c_void_p(16)
+    assert lib.adrt_gb300_adrt(None, fake, 1, 16, 0, None, 0, None) == _lib.ERR_NULL
+    assert lib.adrt_gb300_adrt(fake, fake, 1, 12, 0, None, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_adrt(fake, fake, 0, 16, 0, None, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_adrt(fake, fake, 1, 16, 7, None, 0, None) == _lib.ERR_DTYPE
+    assert lib.adrt_gb300_adrt(fake, fake, 1, 2**30, 0, None, 0, None) == _lib.ERR_TOO_LARGE
+    # n = 1024 needs an intermediate buffer: refused without one.
+    assert lib.adrt_gb300_adrt(fake, fake, 1, 1024, 0, None, 0, None) == _lib.ERR_WORKSPACE
+    assert lib.adrt_gb300_adrt_step(fake, fake, 1, 16, 4, 0, None) == _lib.ERR_STEP
+    assert lib.adrt_gb300_adrt_step(fake, fake, 1, 16, -1, 0, None) == _lib.ERR_STEP
+    assert lib.adrt_gb300_bdrt_step(fake, fake, 1, 16, 4, 0, None) == _lib.ERR_STEP
+    assert lib.adrt_gb300_bdrt(fake, fake, 1, 1024, 1, None, 0, None) == _lib.ERR_WORKSPACE
+    assert lib.adrt_gb300_iadrt(fake, fake, 1, 64, 0, None, 0, None) == _lib.ERR_WORKSPACE
+    assert lib.adrt_gb300_adjoint(fake, fake, 1, 64, 0, None, 0, None) == _lib.ERR_WORKSPACE
+    assert lib.adrt_gb300_fmg_restriction(fake, fake, 1, 1, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_fmg_highpass(fake, fake, 1, 1, 5, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_fmg_prolongation(fake, fake, 1, 0, 5, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_adrt_init(fake, fake, 1, 16, 3, None) == _lib.ERR_DTYPE
+    assert lib.adrt_gb300_elementwise(2, fake, fake, fake, 4, 0, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_sumsq(fake, 4, 0, None, fake, None) == _lib.ERR_NULL
+
+
+def test_workspace_sizes(lib):
+    from adrt_gb300 import _lib
+
+    # One pass (n <= 32) needs no intermediate.
+    assert _lib.workspace_size(_lib.OP_ADRT, 4, 32, _lib.F32) == 0
+    # Two passes: one buffer of 4 n (2n-1) elements per image in the chunk.
+    per = 4 * 1024 * 2047 * 4
+    got = _lib.workspace_size(_lib.OP_ADRT, 256, 1024, _lib.F32)
+    assert got > 0 and got % per == 0
+    assert _lib.workspace_size(_lib.OP_IADRT, 2, 64, _lib.F64) == 2 * 2 * 4 * 64 * 127 * 8
+    with pytest.raises(ValueError):
+        _lib.workspace_size(_lib.OP_ADRT, 1, 12, _lib.F32)
