@@ -199,7 +199,14 @@ static i64 fwd_chunk(i64 batch, i64 n, size_t elem) {
   return k < batch ? k : batch;
 }
 
+// Fast path for float32 at n = 1024 (adrt_fwd_fast.cu).
+bool fast_forward_eligible(i64 n, size_t elem);
+size_t fast_workspace_bytes(i64 batch);
+int adrt_forward_fast(const float *in, float *out, i64 batch, void *ws, size_t ws_bytes,
+                      cudaStream_t st);
+
 size_t fwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
+  if (fast_forward_eligible(n, elem)) return fast_workspace_bytes(batch);
   int sizes[16];
   const int P = plan_passes(num_iters(n), sizes);
   if (P <= 1) return 0;
@@ -210,6 +217,11 @@ size_t fwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
 template <typename T>
 int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (fast_forward_eligible(n, sizeof(T)))
+      return adrt_forward_fast(reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out),
+                               batch, ws, ws_bytes, st);
+  }
   int sizes[16];
   const int P = plan_passes(num_iters(n), sizes);
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);

@@ -1,0 +1,473 @@
+// Fast forward ADRT for float32 at n = 1024 (two passes of five stages).
+//
+// Same decomposition as adrt_fwd.cu: a pass merges 32 members (rows in pass A,
+// row groups in pass B) at input angle a' into 32 angles, member i loaded with
+// the pre-shift a'*i so that only residual shifts remain inside the tile.
+// This kernel keeps those five stages out of shared memory as much as the
+// hardware allows:
+//
+//  group 1 (stages 0-1): each lane owns 4 members x 4 consecutive positions
+//    (one 16-byte chunk per member, loaded straight from global memory with
+//    128-bit loads).  A warp sweeps the tile in iterations of 32 chunks; the
+//    few operands that cross a chunk boundary come from the neighbouring lane
+//    by shuffle, and lane 0 takes them from lane 31's previous iteration.
+//  exchange: the 4 angles x 32 positions of each member quad go to shared
+//    memory (16-byte stores, XOR-swizzled, rows padded to an odd chunk count).
+//  group 2 (stages 2-4): each lane owns 8 combos x 8 positions of one angle
+//    l1 of group 1.  Combo h is read pre-shifted by l1*h, which leaves a fresh
+//    3-stage butterfly with shifts <= 4; boundary operands come from lane-1.
+//
+// Operands whose reference offset is negative are "absent" (the reference
+// copies instead of adding).  They are loaded as -0.0f, and e + (-0) == e bit
+// for bit, so the kernel adds unconditionally and still reproduces the copy.
+// Inductively every value at a negative offset stays -0.0f.
+#include "common.cuh"
+
+namespace adrtg {
+namespace fast {
+
+constexpr int W = 480;            // output offsets per tile
+constexpr int HALO = 32;          // positions left of the outputs
+constexpr int TW = W + HALO;      // 512 tile positions
+constexpr int NCH = TW / 4;       // 128 chunks of 4 positions
+constexpr int RS = 4 * (NCH + 1); // exchange row stride in floats (odd chunk count)
+constexpr int NT = 256;           // threads per CTA
+constexpr int CS = 2048;          // row stride of the intermediate buffer (>= 2n-1, 32-byte multiple)
+constexpr int N = 1024;
+constexpr int C = 2 * N - 1;
+constexpr int COL_TILES = (C + W - 1) / W;  // 5
+constexpr unsigned FULL = 0xffffffffu;
+constexpr size_t SMEM = sizeof(float) * 32 * RS;
+
+__device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float4 ld4_stream(const float *p) {
+  return __ldcs(reinterpret_cast<const float4 *>(p));
+}
+
+__device__ __forceinline__ void st8(float *p, const float (&v)[8]) {
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]),
+               "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
+}
+__device__ __forceinline__ void st8_stream(float *p, const float (&v)[8]) {
+  asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]),
+               "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
+}
+
+// Value of `cur` held by the lane D below (the previous chunk).  Lanes whose
+// previous chunk was handled in the previous iteration (lane < D) receive the
+// `saved` copy from lanes 32-D..31.
+template <int D>
+__device__ __forceinline__ float prev_chunk(float cur, float saved, int lane) {
+  const float send = (lane >= 32 - D) ? saved : cur;
+  return __shfl_sync(FULL, send, (lane - D) & 31);
+}
+
+// ---------------------------------------------------------------------------
+// Group 1: stages 0 and 1 on one member quad, 4 positions.
+//   m[jj][k]  member jj of the quad, position k
+//   o[l1][k]  angle l1 = 2*p0 + p1 of the quad's combo, position k
+// The neighbour values come through `prev`.
+// ---------------------------------------------------------------------------
+struct G1Tail {
+  float m1, m3;          // last position of members 1 and 3
+  float s10, s11a, s11b; // stage-0 odd-pair outputs: li=0 pos 3, li=1 pos 3, li=1 pos 2
+};
+
+template <int D>
+__device__ __forceinline__ void group1_compute(const float (&m)[4][4], float (&o)[4][4],
+                                               G1Tail &saved, int lane) {
+  // stage 0: pairs (0,1) and (2,3); shift p for the odd member.
+  const float pm1 = prev_chunk<D>(m[1][3], saved.m1, lane);
+  const float pm3 = prev_chunk<D>(m[3][3], saved.m3, lane);
+  saved.m1 = m[1][3];
+  saved.m3 = m[3][3];
+  float s0[2][2][4];  // [pair][p][k]
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    s0[0][0][k] = add_rn(m[0][k], m[1][k]);
+    s0[0][1][k] = add_rn(m[0][k], k ? m[1][k - 1] : pm1);
+    s0[1][0][k] = add_rn(m[2][k], m[3][k]);
+    s0[1][1][k] = add_rn(m[2][k], k ? m[3][k - 1] : pm3);
+  }
+  // stage 1: combo 0 (pair 0) + combo 1 (pair 1) shifted by li + p.
+  const float q0 = prev_chunk<D>(s0[1][0][3], saved.s10, lane);   // li=0, position -1
+  const float q1 = prev_chunk<D>(s0[1][1][3], saved.s11a, lane);  // li=1, position -1
+  const float q2 = prev_chunk<D>(s0[1][1][2], saved.s11b, lane);  // li=1, position -2
+  saved.s10 = s0[1][0][3];
+  saved.s11a = s0[1][1][3];
+  saved.s11b = s0[1][1][2];
+  // ext[li][k + 2] = odd combo value at position k (k in [-2, 4))
+  float ext0[6], ext1[6];
+  ext0[0] = 0.f;  // never used (shift <= 1 for li = 0)
+  ext0[1] = q0;
+  ext1[0] = q2;
+  ext1[1] = q1;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ext0[k + 2] = s0[1][0][k];
+    ext1[k + 2] = s0[1][1][k];
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    o[0][k] = add_rn(s0[0][0][k], ext0[k + 2]);      // li=0, p=0
+    o[1][k] = add_rn(s0[0][0][k], ext0[k + 1]);      // li=0, p=1
+    o[2][k] = add_rn(s0[0][1][k], ext1[k + 1]);      // li=1, p=0
+    o[3][k] = add_rn(s0[0][1][k], ext1[k]);          // li=1, p=1
+  }
+}
+
+__device__ __forceinline__ void put_exchange(float *xs, int mq, int ch, const float (&o)[4][4]) {
+#pragma unroll
+  for (int l1 = 0; l1 < 4; ++l1) {
+    float4 v = make_float4(o[l1][0], o[l1][1], o[l1][2], o[l1][3]);
+    *reinterpret_cast<float4 *>(xs + (l1 * 8 + mq) * RS + swz(ch) * 4) = v;
+  }
+}
+
+// Pass A, quadrants 0 and 3: members are image rows, positions run along the
+// row from its right end (offset c <-> column n-1-c).  Warp = member quad.
+__device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase,
+                                                  float *xs) {
+  const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+#pragma unroll 1
+  for (int it = 0; it < NCH / 32; ++it) {
+    const int ch = it * 32 + lane;
+    const int ref0 = tbase + 4 * ch;
+    float m[4][4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int R0 = 32 * r + 4 * mq + jj;
+      const int irow = (q == 0) ? R0 : (N - 1 - R0);
+      if (ref0 < 0) {
+        m[jj][0] = m[jj][1] = m[jj][2] = m[jj][3] = -0.f;
+      } else if (ref0 >= N) {
+        m[jj][0] = m[jj][1] = m[jj][2] = m[jj][3] = 0.f;
+      } else {
+        const float4 v = ld4(img + (size_t)irow * N + (N - 4 - ref0));
+        m[jj][0] = v.w; m[jj][1] = v.z; m[jj][2] = v.y; m[jj][3] = v.x;
+      }
+    }
+    float o[4][4];
+    group1_compute<1>(m, o, saved, lane);
+    put_exchange(xs, mq, ch, o);
+  }
+}
+
+// Pass A, quadrants 1 and 2: members are image columns, positions run down
+// (q2) or up (q1) the columns.  A lane loads one 16-byte row segment (4
+// members) per position and transposes in registers.  Lanes: mq = lane & 7,
+// position group = lane >> 3; warp w sweeps chunks [16w - 1, 16w + 16), the
+// first one only to seed the boundary values.
+__device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r, int tbase,
+                                                  float *xs) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int mq = lane & 7, pg = lane >> 3;
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+#pragma unroll 1
+  for (int it = 0; it < 5; ++it) {
+    const int ch = 16 * w - 1 + 4 * it + pg;
+    const bool live = ch <= 16 * w + 15;
+    const int ref0 = tbase + 4 * ch;
+    float m[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int ref = ref0 + k;
+      if (!live || ref < 0) {
+        m[0][k] = m[1][k] = m[2][k] = m[3][k] = -0.f;
+      } else if (ref >= N) {
+        m[0][k] = m[1][k] = m[2][k] = m[3][k] = 0.f;
+      } else {
+        const int irow = (q == 2) ? ref : (N - 1 - ref);
+        const float4 v = ld4(img + (size_t)irow * N + 32 * r + 4 * mq);
+        m[0][k] = v.x; m[1][k] = v.y; m[2][k] = v.z; m[3][k] = v.w;
+      }
+    }
+    float o[4][4];
+    group1_compute<8>(m, o, saved, lane);
+    if (live && ch >= 16 * w) put_exchange(xs, mq, ch, o);
+  }
+}
+
+// Pass B: members are the 32 row groups of pass A's output at angle a'.
+// Member j's window is shifted by a'*j; a'*j mod 4 = (a' mod 4)*jj mod 4 is a
+// compile-time constant per A4 = a' mod 4, so the realignment is a fixed
+// selection of this lane's and the previous lane's 16-byte chunk.
+template <int A4>
+__device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, float *xs) {
+  const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+  // Seed the chunk that precedes chunk 0 (lane 0 of the first iteration takes
+  // its realignment values from lane 31's saved copy), so that raw values are
+  // exact from tile position 0 on.
+  float wsave[4][4];
+#pragma unroll
+  for (int jj = 0; jj < 4; ++jj) {
+    const int j = 4 * mq + jj;
+    const int g0 = tbase - 4 - 4 * ((ap * j) >> 2);
+    float4 v = make_float4(-0.f, -0.f, -0.f, -0.f);
+    if (g0 >= 0 && g0 < CS) v = ld4_stream(src + (size_t)(j * 32) * CS + g0);
+    wsave[jj][0] = v.x; wsave[jj][1] = v.y; wsave[jj][2] = v.z; wsave[jj][3] = v.w;
+  }
+#pragma unroll 1
+  for (int it = 0; it < NCH / 32; ++it) {
+    const int ch = it * 32 + lane;
+    float m[4][4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = 4 * mq + jj;
+      const int u = (ap * j) >> 2;
+      constexpr int dummy = 0;
+      (void)dummy;
+      const int g0 = tbase + 4 * ch - 4 * u;  // 16-byte aligned column of this lane's chunk
+      float wv[4];
+      if (g0 < 0) {
+        wv[0] = wv[1] = wv[2] = wv[3] = -0.f;
+      } else if (g0 >= CS) {
+        wv[0] = wv[1] = wv[2] = wv[3] = 0.f;
+      } else {
+        const float4 v = ld4_stream(src + (size_t)(j * 32) * CS + g0);
+        wv[0] = v.x; wv[1] = v.y; wv[2] = v.z; wv[3] = v.w;
+      }
+      const int vsh = (A4 * jj) & 3;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k >= vsh) m[jj][k] = wv[k - vsh];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k < vsh) m[jj][k] = prev_chunk<1>(wv[4 - vsh + k], wsave[jj][4 - vsh + k], lane);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) wsave[jj][i] = wv[i];
+    }
+    float o[4][4];
+    group1_compute<1>(m, o, saved, lane);
+    put_exchange(xs, mq, ch, o);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Group 2: stages 2-4 for angle L1 of group 1; lane owns 8 combos x 8
+// positions (block b).  Returns out[l][k], l = local angle (tile angle 8*L1 + l).
+// ---------------------------------------------------------------------------
+template <int L1>
+__device__ __forceinline__ void group2_compute(const float *xs, int b, bool active,
+                                               float (&out)[8][8]) {
+  float r[8][8];
+#pragma unroll
+  for (int h = 0; h < 8; ++h) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int qh = (L1 * h) >> 2, mh = (L1 * h) & 3;
+    float4 B = make_float4(0.f, 0.f, 0.f, 0.f), Cc = B, A = B;
+    const float *row = xs + (L1 * 8 + h) * RS;
+    if (active) {
+      B = *reinterpret_cast<const float4 *>(row + swz(8 + 2 * b - qh) * 4);
+      Cc = *reinterpret_cast<const float4 *>(row + swz(9 + 2 * b - qh) * 4);
+    }
+    // Lane 0 has no left neighbour: it reads the preceding chunk itself.
+    if (mh > 0 && (threadIdx.x & 31) == 0)
+      A = *reinterpret_cast<const float4 *>(row + swz(7 + 2 * b - qh) * 4);
+    const float bv[4] = {B.x, B.y, B.z, B.w};
+    const float cv[4] = {Cc.x, Cc.y, Cc.z, Cc.w};
+    const float av[4] = {A.x, A.y, A.z, A.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < mh) {
+        const float s = __shfl_up_sync(FULL, cv[4 - mh + k], 1);
+        r[h][k] = (threadIdx.x & 31) ? s : av[4 - mh + k];
+      } else if (k - mh < 4) {
+        r[h][k] = bv[k - mh];
+      } else {
+        r[h][k] = cv[k - mh - 4];
+      }
+    }
+  }
+  // stage a: pairs (2P, 2P+1), shift p.
+  float t0[4][2][8];
+#pragma unroll
+  for (int P = 0; P < 4; ++P) {
+    const float pv = __shfl_up_sync(FULL, r[2 * P + 1][7], 1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      t0[P][0][k] = add_rn(r[2 * P][k], r[2 * P + 1][k]);
+      t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
+    }
+  }
+  // stage b: combos (2Q, 2Q+1), li in {0,1}, shift li + p.
+  float t1[2][4][8];
+#pragma unroll
+  for (int Q = 0; Q < 2; ++Q) {
+#pragma unroll
+    for (int li = 0; li < 2; ++li) {
+      float ext[10];  // ext[k + 2] = odd value at position k, k in [-2, 8)
+      ext[0] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][6], 1);
+      ext[1] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][7], 1);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ext[k + 2] = t0[2 * Q + 1][li][k];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const int sh = li + p;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) t1[Q][2 * li + p][k] = add_rn(t0[2 * Q][li][k], ext[k + 2 - sh]);
+      }
+    }
+  }
+  // stage c: li in [0,4), shift li + p.
+#pragma unroll
+  for (int li = 0; li < 4; ++li) {
+    float ext[12];  // ext[k + 4] = odd value at position k, k in [-4, 8)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ext[k] = __shfl_up_sync(FULL, t1[1][li][4 + k], 1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) ext[k + 4] = t1[1][li][k];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int sh = li + p;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[2 * li + p][k] = add_rn(t1[0][li][k], ext[k + 4 - sh]);
+    }
+  }
+}
+
+// Block b of this lane: warps 0-3 (half 0) cover blocks -1..30 (block -1 only
+// seeds the boundary values), warps 4-7 cover 30..61 (block 30 seeds).
+__device__ __forceinline__ void group2_lane(int &b, bool &active, bool &store) {
+  const int lane = threadIdx.x & 31, half = threadIdx.x >> 7;
+  b = half ? 30 + lane : lane - 1;
+  active = b < W / 8;
+  store = active && lane > 0;
+}
+
+template <int L1>
+__device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, int c0) {
+  int b;
+  bool active, store;
+  group2_lane(b, active, store);
+  float out[8][8];
+  group2_compute<L1>(xs, b, active, out);
+  const int d0 = c0 + 8 * b;
+  if (store && d0 < CS) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) st8(dst_rows + (size_t)(8 * L1 + l) * CS + d0, out[l]);
+  }
+}
+
+template <int L1>
+__device__ __forceinline__ void group2_passB(const float *xs, float *dst_q, int ap, int c0) {
+  int b;
+  bool active, store;
+  group2_lane(b, active, store);
+  float out[8][8];
+  group2_compute<L1>(xs, b, active, out);
+  if (!store) return;
+  const int d0 = c0 + 8 * b;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int d = d0 + k;
+    if (d < C) {
+      float v[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) v[l] = out[l][k];
+      st8_stream(dst_q + (size_t)d * N + ap * 32 + 8 * L1, v);
+    }
+  }
+}
+
+// inter layout: [image][q][row group g (32)][angle a (32)][CS]
+__global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__ in,
+                                                       float *__restrict__ inter, int nimg) {
+  extern __shared__ __align__(16) float xs[];
+  int t = blockIdx.x;
+  const int ct = t % COL_TILES; t /= COL_TILES;
+  const int r = t % 32; t /= 32;
+  const int q = t % 4; t /= 4;
+  const int bimg = t;
+  const int c0 = ct * W, tbase = c0 - HALO;
+  const float *img = in + (size_t)bimg * N * N;
+  if (q == 0 || q == 3) group1_passA_rows(img, q, r, tbase, xs);
+  else group1_passA_cols(img, q, r, tbase, xs);
+  __syncthreads();
+  float *dst_rows = inter + ((size_t)(bimg * 4 + q) * 32 + r) * 32 * CS;
+  switch ((threadIdx.x >> 5) & 3) {
+    case 0: group2_passA<0>(xs, dst_rows, c0); break;
+    case 1: group2_passA<1>(xs, dst_rows, c0); break;
+    case 2: group2_passA<2>(xs, dst_rows, c0); break;
+    default: group2_passA<3>(xs, dst_rows, c0); break;
+  }
+}
+
+__global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__ inter,
+                                                       float *__restrict__ out, int nimg) {
+  extern __shared__ __align__(16) float xs[];
+  int t = blockIdx.x;
+  const int ct = t % COL_TILES; t /= COL_TILES;
+  const int ap = t % 32; t /= 32;
+  const int q = t % 4; t /= 4;
+  const int bimg = t;
+  const int c0 = ct * W, tbase = c0 - HALO;
+  // member j row: inter[bimg][q][j][ap][*]
+  const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * 32 + ap) * CS;
+  switch (ap & 3) {
+    case 0: group1_passB<0>(src, ap, tbase, xs); break;
+    case 1: group1_passB<1>(src, ap, tbase, xs); break;
+    case 2: group1_passB<2>(src, ap, tbase, xs); break;
+    default: group1_passB<3>(src, ap, tbase, xs); break;
+  }
+  __syncthreads();
+  float *dst_q = out + (size_t)(bimg * 4 + q) * C * N;
+  switch ((threadIdx.x >> 5) & 3) {
+    case 0: group2_passB<0>(xs, dst_q, ap, c0); break;
+    case 1: group2_passB<1>(xs, dst_q, ap, c0); break;
+    case 2: group2_passB<2>(xs, dst_q, ap, c0); break;
+    default: group2_passB<3>(xs, dst_q, ap, c0); break;
+  }
+}
+
+}  // namespace fast
+
+// Bytes of intermediate per image for the fast path.
+size_t fast_inter_bytes() { return sizeof(float) * 4 * 32 * 32 * fast::CS; }
+
+bool fast_forward_eligible(i64 n, size_t elem) { return n == fast::N && elem == 4; }
+
+// Images per chunk so that the intermediate (33.5 MB per image) stays in L2.
+static i64 fast_chunk(i64 batch) {
+  const i64 k = 2;
+  return batch < k ? batch : k;
+}
+
+size_t fast_workspace_bytes(i64 batch) { return fast_inter_bytes() * (size_t)fast_chunk(batch); }
+
+int adrt_forward_fast(const float *in, float *out, i64 batch, void *ws, size_t ws_bytes,
+                      cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(fast::pass_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
+    cudaFuncSetAttribute(fast::pass_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
+    configured = true;
+  }
+  const i64 per = (i64)fast_inter_bytes();
+  i64 chunk = fast_chunk(batch);
+  if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
+  if ((i64)ws_bytes < per * chunk) chunk = (i64)ws_bytes / per;
+  float *inter = static_cast<float *>(ws);
+  for (i64 b0 = 0; b0 < batch; b0 += chunk) {
+    const int nb = (int)((batch - b0) < chunk ? (batch - b0) : chunk);
+    const unsigned grid = (unsigned)(nb * 4 * 32 * fast::COL_TILES);
+    fast::pass_a_kernel<<<grid, fast::NT, fast::SMEM, st>>>(in + b0 * fast::N * fast::N, inter, nb);
+    int rc = launch_status();
+    if (rc) return rc;
+    fast::pass_b_kernel<<<grid, fast::NT, fast::SMEM, st>>>(inter, out + b0 * 4 * (i64)fast::C * fast::N, nb);
+    rc = launch_status();
+    if (rc) return rc;
+  }
+  return ADRT_GB300_OK;
+}
+
+}  // namespace adrtg
