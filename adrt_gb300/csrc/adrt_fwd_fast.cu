@@ -128,33 +128,41 @@ __device__ __forceinline__ void put_exchange(float *xs, int mq, int ch, const fl
   }
 }
 
+// Loads of group 1 are all issued before any of them is consumed: a warp
+// holds its whole sweep (4-5 chunks per member) in registers, so the load
+// latency is paid once per tile rather than once per iteration.
+
 // Pass A, quadrants 0 and 3: members are image rows, positions run along the
 // row from its right end (offset c <-> column n-1-c).  Warp = member quad.
 __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
-  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
-#pragma unroll 1
-  for (int it = 0; it < NCH / 32; ++it) {
-    const int ch = it * 32 + lane;
-    const int ref0 = tbase + 4 * ch;
-    float m[4][4];
+  constexpr int IT = NCH / 32;
+  float4 raw[IT][4];
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int ref0 = tbase + 4 * (it * 32 + lane);
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
       const int R0 = 32 * r + 4 * mq + jj;
       const int irow = (q == 0) ? R0 : (N - 1 - R0);
-      if (ref0 < 0) {
-        m[jj][0] = m[jj][1] = m[jj][2] = m[jj][3] = -0.f;
-      } else if (ref0 >= N) {
-        m[jj][0] = m[jj][1] = m[jj][2] = m[jj][3] = 0.f;
-      } else {
-        const float4 v = ld4(img + (size_t)irow * N + (N - 4 - ref0));
-        m[jj][0] = v.w; m[jj][1] = v.z; m[jj][2] = v.y; m[jj][3] = v.x;
-      }
+      if (ref0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
+      else if (ref0 >= N) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
+      else raw[it][jj] = ld4(img + (size_t)irow * N + (N - 4 - ref0));
+    }
+  }
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    float m[4][4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      m[jj][0] = raw[it][jj].w; m[jj][1] = raw[it][jj].z;
+      m[jj][2] = raw[it][jj].y; m[jj][3] = raw[it][jj].x;
     }
     float o[4][4];
     group1_compute<1>(m, o, saved, lane);
-    put_exchange(xs, mq, ch, o);
+    put_exchange(xs, mq, it * 32 + lane, o);
   }
 }
 
@@ -167,25 +175,32 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
                                                   float *xs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int mq = lane & 7, pg = lane >> 3;
-  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
-#pragma unroll 1
-  for (int it = 0; it < 5; ++it) {
+  constexpr int IT = 5;
+  float4 raw[IT][4];
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
     const int ch = 16 * w - 1 + 4 * it + pg;
     const bool live = ch <= 16 * w + 15;
     const int ref0 = tbase + 4 * ch;
-    float m[4][4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int ref = ref0 + k;
-      if (!live || ref < 0) {
-        m[0][k] = m[1][k] = m[2][k] = m[3][k] = -0.f;
-      } else if (ref >= N) {
-        m[0][k] = m[1][k] = m[2][k] = m[3][k] = 0.f;
-      } else {
-        const int irow = (q == 2) ? ref : (N - 1 - ref);
-        const float4 v = ld4(img + (size_t)irow * N + 32 * r + 4 * mq);
-        m[0][k] = v.x; m[1][k] = v.y; m[2][k] = v.z; m[3][k] = v.w;
-      }
+      const int irow = (q == 2) ? ref : (N - 1 - ref);
+      if (!live || ref < 0) raw[it][k] = make_float4(-0.f, -0.f, -0.f, -0.f);
+      else if (ref >= N) raw[it][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      else raw[it][k] = ld4(img + (size_t)irow * N + 32 * r + 4 * mq);
+    }
+  }
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int ch = 16 * w - 1 + 4 * it + pg;
+    const bool live = ch <= 16 * w + 15;
+    float m[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      m[0][k] = raw[it][k].x; m[1][k] = raw[it][k].y;
+      m[2][k] = raw[it][k].z; m[3][k] = raw[it][k].w;
     }
     float o[4][4];
     group1_compute<8>(m, o, saved, lane);
@@ -196,58 +211,45 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
 // Pass B: members are the 32 row groups of pass A's output at angle a'.
 // Member j's window is shifted by a'*j; a'*j mod 4 = (a' mod 4)*jj mod 4 is a
 // compile-time constant per A4 = a' mod 4, so the realignment is a fixed
-// selection of this lane's and the previous lane's 16-byte chunk.
+// selection of this lane's and the previous lane's 16-byte chunk.  Slot 0 of
+// `raw` holds the chunk that precedes the first one, seeding lane 0.
 template <int A4>
 __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, float *xs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
-  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
-  // Seed the chunk that precedes chunk 0 (lane 0 of the first iteration takes
-  // its realignment values from lane 31's saved copy), so that raw values are
-  // exact from tile position 0 on.
-  float wsave[4][4];
+  constexpr int IT = NCH / 32;
+  float4 raw[IT + 1][4];
 #pragma unroll
   for (int jj = 0; jj < 4; ++jj) {
     const int j = 4 * mq + jj;
-    const int g0 = tbase - 4 - 4 * ((ap * j) >> 2);
-    float4 v = make_float4(-0.f, -0.f, -0.f, -0.f);
-    if (g0 >= 0 && g0 < CS) v = ld4_stream(src + (size_t)(j * 32) * CS + g0);
-    wsave[jj][0] = v.x; wsave[jj][1] = v.y; wsave[jj][2] = v.z; wsave[jj][3] = v.w;
+    const float *row = src + (size_t)(j * 32) * CS;
+    const int gb = tbase - 4 * ((ap * j) >> 2);
+#pragma unroll
+    for (int it = 0; it <= IT; ++it) {
+      // slot 0: the chunk before chunk 0 (only lane 31's copy is used)
+      const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
+      if (g0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
+      else if (g0 >= CS) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
+      else raw[it][jj] = ld4_stream(row + g0);
+    }
   }
-#pragma unroll 1
-  for (int it = 0; it < NCH / 32; ++it) {
-    const int ch = it * 32 + lane;
+  G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
+#pragma unroll
+  for (int it = 1; it <= IT; ++it) {
     float m[4][4];
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
-      const int j = 4 * mq + jj;
-      const int u = (ap * j) >> 2;
-      constexpr int dummy = 0;
-      (void)dummy;
-      const int g0 = tbase + 4 * ch - 4 * u;  // 16-byte aligned column of this lane's chunk
-      float wv[4];
-      if (g0 < 0) {
-        wv[0] = wv[1] = wv[2] = wv[3] = -0.f;
-      } else if (g0 >= CS) {
-        wv[0] = wv[1] = wv[2] = wv[3] = 0.f;
-      } else {
-        const float4 v = ld4_stream(src + (size_t)(j * 32) * CS + g0);
-        wv[0] = v.x; wv[1] = v.y; wv[2] = v.z; wv[3] = v.w;
-      }
+      const float wv[4] = {raw[it][jj].x, raw[it][jj].y, raw[it][jj].z, raw[it][jj].w};
+      const float pv[4] = {raw[it - 1][jj].x, raw[it - 1][jj].y, raw[it - 1][jj].z, raw[it - 1][jj].w};
       const int vsh = (A4 * jj) & 3;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (k >= vsh) m[jj][k] = wv[k - vsh];
+        else m[jj][k] = prev_chunk<1>(wv[4 - vsh + k], pv[4 - vsh + k], lane);
       }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k < vsh) m[jj][k] = prev_chunk<1>(wv[4 - vsh + k], wsave[jj][4 - vsh + k], lane);
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i) wsave[jj][i] = wv[i];
     }
     float o[4][4];
     group1_compute<1>(m, o, saved, lane);
-    put_exchange(xs, mq, ch, o);
+    put_exchange(xs, mq, (it - 1) * 32 + lane, o);
   }
 }
 
