@@ -278,23 +278,24 @@ def main():
     del y
 
     # ---- end to end through host buffers ----------------------------------
-    xh = x.cpu().pin_memory()
-    for _ in range(1):
+    e2e = None
+    if args.e2e_steps > 0:
+        xh = x.cpu().pin_memory()
         yh = adrt.adrt(xh)
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        yh = adrt.adrt(xh)
-    torch.cuda.synchronize()
-    t_e2e = max_over_ranks(time.perf_counter() - t0)
-    e2e = {
-        "value": world * B * args.e2e_steps / t_e2e,
-        "unit": UNIT,
-        "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
-        "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
-    }
-    del yh
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            yh = adrt.adrt(xh)
+        torch.cuda.synchronize()
+        t_e2e = max_over_ranks(time.perf_counter() - t0)
+        e2e = {
+            "value": world * B * args.e2e_steps / t_e2e,
+            "unit": UNIT,
+            "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
+            "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
+        }
+        del yh
 
     extras = {}
     if not args.no_extras:
@@ -365,7 +366,7 @@ def main():
         "clocks": clocks,
     }
     line.update(extras)
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:
         line["cpu_baseline"] = cpu_baseline_run(n, "float32", args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)

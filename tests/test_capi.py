@@ -92,10 +92,14 @@ def test_workspace_sizes(lib):
 
     # One pass (n <= 32) needs no intermediate.
     assert _lib.workspace_size(_lib.OP_ADRT, 4, 32, _lib.F32) == 0
-    # Two passes: one buffer of 4 n (2n-1) elements per image in the chunk.
-    per = 4 * 1024 * 2047 * 4
+    # Two passes: one intermediate per image in the chunk; the fast float32
+    # path pads rows of 2n-1 = 2047 offsets to 2048.
+    per = 4 * 32 * 32 * 2048 * 4
     got = _lib.workspace_size(_lib.OP_ADRT, 256, 1024, _lib.F32)
     assert got > 0 and got % per == 0
+    per64 = 4 * 512 * 1023 * 8
+    got64 = _lib.workspace_size(_lib.OP_ADRT, 8, 512, _lib.F64)
+    assert got64 > 0 and got64 % per64 == 0
     assert _lib.workspace_size(_lib.OP_IADRT, 2, 64, _lib.F64) == 2 * 2 * 4 * 64 * 127 * 8
     with pytest.raises(ValueError):
         _lib.workspace_size(_lib.OP_ADRT, 1, 12, _lib.F32)
