@@ -47,6 +47,7 @@ SIGNATURES = {
     "adrt_gb300_launch_count": [],
     "adrt_gb300_workspace_size": [_int, _i64, _i64, _int, ctypes.POINTER(_sz)],
     "adrt_gb300_adrt": [_v, _v, _i64, _i64, _int, _v, _sz, _v],
+    "adrt_gb300_adrt_noalloc": [_v, _v, _i64, _i64, _int, _v],
     "adrt_gb300_adrt_step": [_v, _v, _i64, _i64, _int, _int, _v],
     "adrt_gb300_bdrt": [_v, _v, _i64, _i64, _int, _v, _sz, _v],
     "adrt_gb300_bdrt_step": [_v, _v, _i64, _i64, _int, _int, _v],

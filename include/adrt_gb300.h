@@ -76,6 +76,20 @@ int adrt_gb300_workspace_size(int op, int64_t batch, int64_t n, int dtype, size_
 int adrt_gb300_adrt(const void *in, void *out, int64_t batch, int64_t n, int dtype,
                     void *workspace, size_t workspace_bytes, void *stream);
 
+/* Forward ADRT that allocates nothing and takes no workspace; no counterpart
+ * in the reference.  For callers that are given input and output buffers but
+ * may not allocate device memory (a fixed memory budget reserved at start-up,
+ * a host framework that owns the pool, a binding without an allocator).  Its
+ * intermediate is a static device array of ADRT_GB300_NOALLOC_SCRATCH_BYTES
+ * that each GPU loading this library holds until exit; the first call on a
+ * device looks up that array's address (make that first call before any
+ * stream capture).  Sizes whose per-image intermediate exceeds the scratch
+ * (float32 n >= 2048, float64 n >= 1024) return ADRT_GB300_ERR_TOO_LARGE.
+ * All calls share the scratch: calls that overlap on the GPU race. */
+#define ADRT_GB300_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int adrt_gb300_adrt_noalloc(const void *in, void *out, int64_t batch, int64_t n, int dtype,
+                            void *stream);
+
 /* One forward stage in the output layout: (batch, 4, 2n-1, n) -> same.
  * Replaces adrt::adrt_step (src/adrt/adrt_cdefs_adrt.hpp:215-258),
  * bound as _adrt_cdefs.adrt_step (src/adrt/adrt_cdefs_py.cpp:343-412). */
