@@ -63,11 +63,16 @@ SIGNATURES = {
     "adrt_gb300_elementwise": [_int, _v, _v, _v, _i64, _int, _v],
     "adrt_gb300_sumsq_workspace_size": [],
     "adrt_gb300_sumsq": [_v, _i64, _int, _v, _v, _v],
+    "adrt_gb300_cg_workspace_size": [_i64],
+    "adrt_gb300_batched_dot": [_v, _v, _v, _i64, _i64, _int, _v, _v],
+    "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
+    "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
 }
 _RESTYPES = {
     "adrt_gb300_status_string": ctypes.c_char_p,
     "adrt_gb300_sumsq_workspace_size": _sz,
     "adrt_gb300_launch_count": ctypes.c_uint64,
+    "adrt_gb300_cg_workspace_size": _sz,
 }
 
 

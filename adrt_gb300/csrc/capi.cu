@@ -17,6 +17,13 @@ template <typename T> int fmg_correction_launch(const T *, T *, i64, i64, cudaSt
 template <typename T> int binary_launch(const T *, const T *, T *, i64, int, cudaStream_t);
 template <typename T> int sumsq_launch(const T *, i64, double *, void *, cudaStream_t);
 size_t sumsq_workspace_bytes();
+size_t cg_workspace_bytes(i64);
+template <typename T> int batched_dot_launch(const T *, const T *, double *, i64, i64, void *, cudaStream_t);
+template <typename T>
+int cg_update_launch(T *, T *, const T *, const T *, const double *, const double *, const int *,
+                     double *, i64, i64, void *, cudaStream_t);
+template <typename T>
+int cg_direction_launch(T *, const T *, const double *, double *, const int *, i64, i64, cudaStream_t);
 size_t fwd_workspace_bytes(i64, i64, size_t);
 size_t bwd_workspace_bytes(i64, i64, size_t);
 size_t iadrt_workspace_bytes(i64, i64, size_t);
@@ -259,6 +266,48 @@ int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void 
   return DISPATCH(dtype,
                   sumsq_launch<float>((const float *)a, count, out, ws, S(stream)),
                   sumsq_launch<double>((const double *)a, count, out, ws, S(stream)));
+}
+
+}  // extern "C"
+
+extern "C" {
+
+size_t adrt_gb300_cg_workspace_size(int64_t batch) { return batch > 0 ? cg_workspace_bytes(batch) : 0; }
+
+int adrt_gb300_batched_dot(const void *a, const void *b, double *out, int64_t batch, int64_t per,
+                           int dtype, void *ws, void *stream) {
+  int rc;
+  if (!a || !b || !out || !ws) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (batch < 1 || batch > 65535 || per < 1) return ADRT_GB300_ERR_SHAPE;
+  return DISPATCH(dtype,
+                  batched_dot_launch<float>((const float *)a, (const float *)b, out, batch, per, ws, S(stream)),
+                  batched_dot_launch<double>((const double *)a, (const double *)b, out, batch, per, ws, S(stream)));
+}
+
+int adrt_gb300_cg_update(void *x, void *r, const void *p, const void *Ap, const double *rs,
+                         const double *pAp, const int *active, double *rs_new, int64_t batch,
+                         int64_t per, int dtype, void *ws, void *stream) {
+  int rc;
+  if (!x || !r || !p || !Ap || !rs || !pAp || !active || !rs_new || !ws) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (batch < 1 || batch > 65535 || per < 1) return ADRT_GB300_ERR_SHAPE;
+  return DISPATCH(dtype,
+                  cg_update_launch<float>((float *)x, (float *)r, (const float *)p, (const float *)Ap, rs, pAp,
+                                          active, rs_new, batch, per, ws, S(stream)),
+                  cg_update_launch<double>((double *)x, (double *)r, (const double *)p, (const double *)Ap, rs,
+                                           pAp, active, rs_new, batch, per, ws, S(stream)));
+}
+
+int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double *rs,
+                            const int *active, int64_t batch, int64_t per, int dtype, void *stream) {
+  int rc;
+  if (!p || !r || !rs_new || !rs || !active) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (batch < 1 || batch > 65535 || per < 1) return ADRT_GB300_ERR_SHAPE;
+  return DISPATCH(dtype,
+                  cg_direction_launch<float>((float *)p, (const float *)r, rs_new, rs, active, batch, per, S(stream)),
+                  cg_direction_launch<double>((double *)p, (const double *)r, rs_new, rs, active, batch, per, S(stream)));
 }
 
 }  // extern "C"

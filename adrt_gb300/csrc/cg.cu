@@ -1,0 +1,138 @@
+// Batched conjugate-gradient vector kernels for the ADRT normal equations.
+//
+// Every image of a batch runs its own CG recurrence; scalars (dot products,
+// alpha, beta) are per image and accumulated in float64 in a fixed order
+// (fixed grid, fixed per-thread stride, fixed shared-memory tree), so results
+// do not depend on scheduling.  An image whose `active` flag is 0 is frozen:
+// its alpha is 0 and its direction is left unchanged.
+#include "common.cuh"
+
+namespace adrtg {
+
+constexpr int kDotThreads = 256;
+constexpr int kDotBlocksPerImage = 32;
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kDotThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  return sh[0];
+}
+
+// partial[img][blk] = sum over the block's strided slice of a*b.
+template <typename T>
+__global__ void dot_partial_kernel(const T *__restrict__ a, const T *__restrict__ b, i64 per,
+                                   double *partial) {
+  __shared__ double sh[kDotThreads];
+  const int img = blockIdx.y, blk = blockIdx.x;
+  const T *pa = a + (i64)img * per, *pb = b + (i64)img * per;
+  double acc = 0.0;
+  for (i64 i = (i64)blk * kDotThreads + threadIdx.x; i < per; i += (i64)kDotBlocksPerImage * kDotThreads)
+    acc = __dadd_rn(acc, __dmul_rn((double)pa[i], (double)pb[i]));
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[img * kDotBlocksPerImage + blk] = s;
+}
+
+__global__ void dot_final_kernel(const double *partial, double *out, int batch) {
+  const int img = blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= batch) return;
+  double s = 0.0;
+  for (int k = 0; k < kDotBlocksPerImage; ++k) s = __dadd_rn(s, partial[img * kDotBlocksPerImage + k]);
+  out[img] = s;
+}
+
+// alpha = rs / pAp (0 if frozen or pAp == 0); x += alpha p; r -= alpha Ap;
+// partial sums of r*r for rs_new.
+template <typename T>
+__global__ void cg_update_kernel(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                                 const T *__restrict__ Ap, const double *rs, const double *pAp,
+                                 const int *active, i64 per, double *partial) {
+  __shared__ double sh[kDotThreads];
+  const int img = blockIdx.y, blk = blockIdx.x;
+  const double den = pAp[img];
+  const bool on = active[img] != 0 && den != 0.0;
+  const T alpha = on ? (T)(rs[img] / den) : T(0);
+  T *px = x + (i64)img * per, *pr = r + (i64)img * per;
+  const T *pp = p + (i64)img * per, *pAp_ = Ap + (i64)img * per;
+  double acc = 0.0;
+  for (i64 i = (i64)blk * kDotThreads + threadIdx.x; i < per; i += (i64)kDotBlocksPerImage * kDotThreads) {
+    T rv = pr[i];
+    if (on) {
+      px[i] = add_rn(px[i], mul_rn(alpha, pp[i]));
+      rv = sub_rn(rv, mul_rn(alpha, pAp_[i]));
+      pr[i] = rv;
+    }
+    acc = __dadd_rn(acc, __dmul_rn((double)rv, (double)rv));
+  }
+  const double s = block_sum(acc, sh);
+  if (threadIdx.x == 0) partial[img * kDotBlocksPerImage + blk] = s;
+}
+
+// beta = rs_new / rs; p = r + beta p; rs = rs_new (active images only).
+template <typename T>
+__global__ void cg_direction_kernel(T *__restrict__ p, const T *__restrict__ r, const double *rs_new,
+                                    double *rs, const int *active, i64 per) {
+  const int img = blockIdx.y;
+  if (!active[img]) return;
+  const double old = rs[img];
+  const T beta = old != 0.0 ? (T)(rs_new[img] / old) : T(0);
+  T *pp = p + (i64)img * per;
+  const T *pr = r + (i64)img * per;
+  for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < per; i += (i64)gridDim.x * blockDim.x)
+    pp[i] = add_rn(pr[i], mul_rn(beta, pp[i]));
+}
+
+__global__ void cg_commit_kernel(double *rs, const double *rs_new, const int *active, int batch) {
+  const int img = blockIdx.x * blockDim.x + threadIdx.x;
+  if (img < batch && active[img]) rs[img] = rs_new[img];
+}
+
+size_t cg_workspace_bytes(i64 batch) { return sizeof(double) * (size_t)batch * kDotBlocksPerImage; }
+
+template <typename T>
+int batched_dot_launch(const T *a, const T *b, double *out, i64 batch, i64 per, void *ws,
+                       cudaStream_t st) {
+  double *partial = static_cast<double *>(ws);
+  dot_partial_kernel<T><<<dim3(kDotBlocksPerImage, (unsigned)batch), kDotThreads, 0, st>>>(a, b, per, partial);
+  int rc = launch_status();
+  if (rc) return rc;
+  dot_final_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(partial, out, (int)batch);
+  return launch_status();
+}
+
+template <typename T>
+int cg_update_launch(T *x, T *r, const T *p, const T *Ap, const double *rs, const double *pAp,
+                     const int *active, double *rs_new, i64 batch, i64 per, void *ws, cudaStream_t st) {
+  double *partial = static_cast<double *>(ws);
+  cg_update_kernel<T><<<dim3(kDotBlocksPerImage, (unsigned)batch), kDotThreads, 0, st>>>(
+      x, r, p, Ap, rs, pAp, active, per, partial);
+  int rc = launch_status();
+  if (rc) return rc;
+  dot_final_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(partial, rs_new, (int)batch);
+  return launch_status();
+}
+
+template <typename T>
+int cg_direction_launch(T *p, const T *r, const double *rs_new, double *rs, const int *active,
+                        i64 batch, i64 per, cudaStream_t st) {
+  cg_direction_kernel<T><<<dim3(32, (unsigned)batch), 256, 0, st>>>(p, r, rs_new, rs, active, per);
+  int rc = launch_status();
+  if (rc) return rc;
+  cg_commit_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(rs, rs_new, active, (int)batch);
+  return launch_status();
+}
+
+#define INST(T)                                                                                \
+  template int batched_dot_launch<T>(const T *, const T *, double *, i64, i64, void *, cudaStream_t); \
+  template int cg_update_launch<T>(T *, T *, const T *, const T *, const double *, const double *, \
+                                   const int *, double *, i64, i64, void *, cudaStream_t);     \
+  template int cg_direction_launch<T>(T *, const T *, const double *, double *, const int *, i64, \
+                                      i64, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace adrtg

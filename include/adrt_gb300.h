@@ -179,6 +179,29 @@ size_t adrt_gb300_sumsq_workspace_size(void);
 int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void *workspace,
                      void *stream);
 
+/* ---- Batched conjugate gradient on the normal equations A^T A x = A^T b.
+ * The reference documents this solve as a SciPy recipe
+ * (docs/examples.cginverse.md:40-67); these kernels run its vector algebra for
+ * a whole batch on the device.  Per-image scalars are float64, accumulated in
+ * a fixed order (deterministic).  `per` = elements per image.  Images whose
+ * active[i] == 0 are left unchanged. ------------------------------------ */
+
+/* Bytes of workspace the CG kernels need for `batch` images. */
+size_t adrt_gb300_cg_workspace_size(int64_t batch);
+
+/* out[i] = sum_k a[i,k] * b[i,k] (float64). */
+int adrt_gb300_batched_dot(const void *a, const void *b, double *out, int64_t batch, int64_t per,
+                           int dtype, void *workspace, void *stream);
+
+/* alpha_i = rs[i] / pAp[i]; x += alpha p; r -= alpha Ap; rs_new[i] = <r, r>. */
+int adrt_gb300_cg_update(void *x, void *r, const void *p, const void *Ap, const double *rs,
+                         const double *pAp, const int *active, double *rs_new, int64_t batch,
+                         int64_t per, int dtype, void *workspace, void *stream);
+
+/* beta_i = rs_new[i] / rs[i]; p = r + beta p; rs[i] = rs_new[i]. */
+int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double *rs,
+                            const int *active, int64_t batch, int64_t per, int dtype, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
