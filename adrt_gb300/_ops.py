@@ -15,6 +15,8 @@ from ._wrappers import (
     check_nonzero,
     ensure_cuda,
     float_code,
+    host_pipeline,
+    is_host,
     is_pow2,
     ptr,
     valid_adrt_output_shape,
@@ -37,8 +39,10 @@ def adrt(a, /):
         raise ValueError("array must be square with a power of two shape")
     code = float_code(a)
     ensure_cuda()
-    st = Staged(a)
     n = int(a.shape[-1])
+    if is_host(a) and a.ndim == 3 and a.shape[0] > 1:
+        return _host_batched(a, _lib.OP_ADRT, "adrt_gb300_adrt", n, code, (4, 2 * n - 1, n))
+    st = Staged(a)
     b = batch_of(a.shape, 2)
     out = st.empty((*a.shape[:-2], 4, 2 * n - 1, n))
     ws, nbytes = workspace(st, _lib.OP_ADRT, b, n, code)
@@ -94,12 +98,38 @@ def _num_iters_int(n: int) -> int:
     return n.bit_length() - (1 if n > 0 and (n & (n - 1)) == 0 else 0)
 
 
+def _host_chunk(n: int, elem: int) -> int:
+    """Images per pipeline chunk for host inputs: about 256 MB of output."""
+    per = 4 * n * (2 * n - 1) * elem
+    return max(1, (256 << 20) // per)
+
+
+def _host_batched(a, op, fn, n, code, out_tail):
+    """Host batch: chunked device transform with overlapped copies."""
+    import torch
+
+    elem = 4 if code == _lib.F32 else 8
+    chunk = min(_host_chunk(n, elem), int(a.shape[0]))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nbytes = _lib.workspace_size(op, chunk, n, code)
+    ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+    lib = _lib.load()
+
+    def run(d_in, d_out, k, stream):
+        rc = getattr(lib, fn)(ptr(d_in), ptr(d_out), k, n, code, ptr(ws), nbytes, stream)
+        _lib.check(rc, fn)
+
+    return host_pipeline(a, out_tail, chunk, run)
+
+
 def _transform3(a, op, fn, name):
     _adrt_shaped_prologue(a, "array must have a valid ADRT output shape")
     code = float_code(a)
     ensure_cuda()
-    st = Staged(a)
     n = int(a.shape[-1])
+    if is_host(a) and a.ndim == 4 and a.shape[0] > 1:
+        return _host_batched(a, op, fn, n, code, (4, 2 * n - 1, n))
+    st = Staged(a)
     b = batch_of(a.shape, 3)
     out = st.empty(tuple(a.shape))
     ws, nbytes = workspace(st, op, b, n, code)

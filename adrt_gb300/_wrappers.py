@@ -118,6 +118,66 @@ class Staged:
         return torch.cuda.current_stream(self.device).cuda_stream
 
 
+def is_host(a) -> bool:
+    return isinstance(a, np.ndarray) or (isinstance(a, torch.Tensor) and not a.is_cuda)
+
+
+def host_pipeline(a, out_tail, chunk, run_chunk):
+    """Transform a host array batch by batch with copies overlapped.
+
+    `a` is a host array (NumPy or CPU tensor) of shape (B, *in_tail).  The
+    batch is split into chunks of `chunk` images; chunk i's host-to-device
+    copy, chunk i-1's transform and chunk i-2's device-to-host copy run on
+    three streams at once, through two device buffers.  The result is written
+    into pinned host memory (torch's caching host allocator, so repeated calls
+    reuse it) and returned as the caller's kind (NumPy array or CPU tensor).
+    `run_chunk(d_in, d_out, k, stream_handle)` enqueues the transform of k
+    images on the given stream.
+    """
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if isinstance(a, np.ndarray):
+        host = np.ascontiguousarray(a, dtype=a.dtype.newbyteorder("="))
+        hin = torch.from_numpy(host if host.flags.writeable else host.copy())
+    else:
+        hin = a.contiguous()
+    B = hin.shape[0]
+    hout = torch.empty((B, *out_tail), dtype=hin.dtype, pin_memory=True)
+    cur = torch.cuda.current_stream(dev)
+    s_in, s_run, s_out = (torch.cuda.Stream(device=dev) for _ in range(3))
+    for s in (s_in, s_run, s_out):
+        s.wait_stream(cur)
+    k0 = min(chunk, B)
+    with torch.cuda.stream(s_run):
+        din = [torch.empty((k0, *hin.shape[1:]), dtype=hin.dtype, device=dev) for _ in range(2)]
+        dout = [torch.empty((k0, *out_tail), dtype=hin.dtype, device=dev) for _ in range(2)]
+    in_done = [torch.cuda.Event() for _ in range(2)]
+    run_done = [None, None]
+    out_done = [None, None]
+    for i, b0 in enumerate(range(0, B, k0)):
+        k = min(k0, B - b0)
+        j = i & 1
+        if run_done[j] is not None:
+            s_in.wait_event(run_done[j])      # transform i-2 finished reading din[j]
+        with torch.cuda.stream(s_in):
+            din[j][:k].copy_(hin[b0:b0 + k], non_blocking=True)
+        in_done[j].record(s_in)
+        s_run.wait_event(in_done[j])
+        if out_done[j] is not None:
+            s_run.wait_event(out_done[j])     # copy-out of chunk i-2 finished reading dout[j]
+        run_chunk(din[j][:k], dout[j][:k], k, s_run.cuda_stream)
+        run_done[j] = torch.cuda.Event()
+        run_done[j].record(s_run)
+        s_out.wait_event(run_done[j])
+        with torch.cuda.stream(s_out):
+            hout[b0:b0 + k].copy_(dout[j][:k], non_blocking=True)
+        out_done[j] = torch.cuda.Event()
+        out_done[j].record(s_out)
+    s_out.synchronize()
+    s_run.synchronize()
+    s_in.synchronize()
+    return hout.numpy() if isinstance(a, np.ndarray) else hout
+
+
 def ensure_cuda() -> None:
     if not torch.cuda.is_available():
         raise RuntimeError("adrt_gb300 requires a CUDA device; there is no CPU fallback")

@@ -35,16 +35,30 @@ struct FwdPassArgs {
   i64 n;           // image side
   int k0;          // index of the first stage of this pass
   i64 batch;
+  i64 cs_out = 0;  // row stride of a non-final output buffer (0: 2n-1)
+};
+
+// Shared-memory rows of one tile.  During a stage each thread owns one output
+// row and every lanes-per-row'th position of it; the row stride is padded so
+// that the rows a warp covers start in different banks.
+template <int ROWS>
+struct FwdTile {
+  static constexpr int TWP = kFwdW + kFwdHalo;          // positions per row
+  static constexpr int LPR = kFwdThreads / ROWS;        // threads per row
+  static constexpr int RPW = LPR >= 32 ? 1 : 32 / LPR;  // rows per warp
+  static constexpr int RS = TWP + (RPW > 1 ? 32 / RPW : 0);
+  static constexpr int BUF = ROWS * RS;
 };
 
 template <typename T, int S, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kFwdThreads)
 fwd_pass_kernel(FwdPassArgs args) {
   constexpr int ROWS = 1 << S;
-  constexpr int TWP = kFwdW + kFwdHalo;
+  using TL = FwdTile<ROWS>;
+  constexpr int TWP = TL::TWP, RS = TL::RS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf0 = reinterpret_cast<T *>(smem_raw);
-  T *buf1 = buf0 + ROWS * TWP;
+  T *buf1 = buf0 + TL::BUF;
 
   const i64 n = args.n;
   const i64 C = 2 * n - 1;
@@ -65,7 +79,11 @@ fwd_pass_kernel(FwdPassArgs args) {
   const i64 c0 = (i64)ct * kFwdW;
   const i64 tbase = c0 - kFwdHalo;  // reference offset of tile position 0 (before pre-shift)
 
-  // ---- load: member i, tile position u  <->  reference offset tbase + u - a'*i
+  // ---- load: member i, tile position u  <->  reference offset tbase + u - a'*i.
+  // Offsets below 0 do not exist in the reference (it copies instead of adding
+  // there); they are stored as -0.0, and e + (-0) == e for every e, so the
+  // stages below add unconditionally.  Offsets n..2n-2 of the first pass are
+  // the reference's +0 padding.
   if (FIRST) {
     const T *img = static_cast<const T *>(args.in) + b * n * n;
     const bool col_major = (q == 1 || q == 2);
@@ -75,7 +93,7 @@ fwd_pass_kernel(FwdPassArgs args) {
       else { i = idx / TWP; u = idx % TWP; }
       const i64 ref = tbase + u;  // a' == 0 in the first pass
       const i64 R0 = r * ROWS + i;
-      T v = T(0);
+      T v = ref < 0 ? T(-0.0) : T(0);
       if (ref >= 0 && ref < n) {
         switch (q) {
           case 0: v = img[R0 * n + (n - 1 - ref)]; break;
@@ -84,7 +102,7 @@ fwd_pass_kernel(FwdPassArgs args) {
           default: v = img[(n - 1 - R0) * n + (n - 1 - ref)]; break;
         }
       }
-      buf0[i * TWP + u] = v;
+      buf0[i * RS + u] = v;
     }
   } else {
     const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * R_in * A_in * C;
@@ -92,34 +110,26 @@ fwd_pass_kernel(FwdPassArgs args) {
       const int i = idx / TWP, u = idx % TWP;
       const i64 ref = tbase + u - ap * i;
       const i64 row = (r * ROWS + i) * A_in + ap;
-      T v = T(0);
+      T v = ref < 0 ? T(-0.0) : T(0);
       if (ref >= 0 && ref < C) v = src[row * C + ref];
-      buf0[i * TWP + u] = v;
+      buf0[i * RS + u] = v;
     }
   }
   __syncthreads();
 
-  // ---- S stages in shared memory.
+  // ---- S stages in shared memory: row m*2A + 2li + p of the output is
+  // row 2m*A + li plus row (2m+1)*A + li shifted by li + p.
   T *cur = buf0, *nxt = buf1;
+  const int rowo = threadIdx.x / TL::LPR, lr = threadIdx.x % TL::LPR;
 #pragma unroll
   for (int j = 0; j < S; ++j) {
-    const int Al_in = 1 << j;
-    const int Rl_out = ROWS >> (j + 1);
-    const int Al_out = Al_in * 2;
-    for (int idx = threadIdx.x; idx < Rl_out * Al_out * TWP; idx += blockDim.x) {
-      const int u = idx % TWP;
-      const int row_out = idx / TWP;
-      const int m = row_out / Al_out, lo = row_out % Al_out;
-      const int li = lo >> 1, sh = li + (lo & 1);
-      const T e = cur[((2 * m) * Al_in + li) * TWP + u];
-      T v = e;
-      if (u >= sh) {
-        // Reference offset of the odd operand (member (2m+1)*2^j pre-shifted by a'*(2m+1)*2^j).
-        const i64 ref_odd = tbase + (u - sh) - ap * (i64)((2 * m + 1) << j);
-        if (ref_odd >= 0) v = add_rn(e, cur[((2 * m + 1) * Al_in + li) * TWP + (u - sh)]);
-      }
-      nxt[row_out * TWP + u] = v;
-    }
+    const int Al_in = 1 << j, Al_out = 2 << j;
+    const int m = rowo / Al_out, lo = rowo % Al_out;
+    const int li = lo >> 1, sh = li + (lo & 1);
+    const T *ep = cur + ((2 * m) * Al_in + li) * RS;
+    const T *op = cur + ((2 * m + 1) * Al_in + li) * RS - sh;  // row index >= 1, so in bounds
+    T *np = nxt + rowo * RS;
+    for (int u = lr; u < TWP; u += TL::LPR) np[u] = add_rn(ep[u], op[u]);
     __syncthreads();
     T *tmp = cur; cur = nxt; nxt = tmp;
   }
@@ -131,14 +141,15 @@ fwd_pass_kernel(FwdPassArgs args) {
     for (int idx = threadIdx.x; idx < kFwdW * ROWS; idx += blockDim.x) {
       const int l = idx % ROWS, w = idx / ROWS;
       const i64 c = c0 + w;
-      if (c < C) st_stream(&dst[c * n + ap * ROWS + l], cur[l * TWP + kFwdHalo + w]);
+      if (c < C) st_stream(&dst[c * n + ap * ROWS + l], cur[l * RS + kFwdHalo + w]);
     }
   } else {
-    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * R_out * A_out * C;
+    const i64 cs = args.cs_out ? args.cs_out : C;
+    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * R_out * A_out * cs;
     for (int idx = threadIdx.x; idx < ROWS * kFwdW; idx += blockDim.x) {
       const int l = idx / kFwdW, w = idx % kFwdW;
       const i64 c = c0 + w;
-      if (c < C) dst[(r * A_out + ap * ROWS + l) * C + c] = cur[l * TWP + kFwdHalo + w];
+      if (c < C) dst[(r * A_out + ap * ROWS + l) * cs + c] = cur[l * RS + kFwdHalo + w];
     }
   }
 }
@@ -156,7 +167,7 @@ static int plan_passes(int L, int *sizes) {
 template <typename T, int S, bool FIRST, bool LAST>
 static int launch_fwd_pass(const FwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S;
-  const size_t smem = 2 * sizeof(T) * ROWS * (kFwdW + kFwdHalo);
+  const size_t smem = 2 * sizeof(T) * FwdTile<ROWS>::BUF;
   auto kern = fwd_pass_kernel<T, S, FIRST, LAST>;
   static bool configured = false;  // per-instantiation, host-side only
   if (!configured) {
@@ -199,14 +210,20 @@ static i64 fwd_chunk(i64 batch, i64 n, size_t elem) {
   return k < batch ? k : batch;
 }
 
-// Fast path for float32 at n = 1024 (adrt_fwd_fast.cu).
+// Fast path for float32, 64 <= n <= 1024 (adrt_fwd_fast.cu).
 bool fast_forward_eligible(i64 n, size_t elem);
-size_t fast_workspace_bytes(i64 batch);
-int adrt_forward_fast(const float *in, float *out, i64 batch, void *ws, size_t ws_bytes,
+size_t fast_workspace_bytes(i64 batch, i64 n);
+int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                       cudaStream_t st);
 
+int fwd_first_pass_padded(const float *in, float *inter, i64 batch, i64 n, int stages, int cs,
+                          cudaStream_t st) {
+  FwdPassArgs a{in, inter, n, 0, batch, cs};
+  return dispatch_pass<float>(stages, true, false, a, st);
+}
+
 size_t fwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
-  if (fast_forward_eligible(n, elem)) return fast_workspace_bytes(batch);
+  if (fast_forward_eligible(n, elem)) return fast_workspace_bytes(batch, n);
   int sizes[16];
   const int P = plan_passes(num_iters(n), sizes);
   if (P <= 1) return 0;
@@ -220,7 +237,7 @@ int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   if constexpr (sizeof(T) == 4) {
     if (fast_forward_eligible(n, sizeof(T)))
       return adrt_forward_fast(reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out),
-                               batch, ws, ws_bytes, st);
+                               batch, n, ws, ws_bytes, st);
   }
   int sizes[16];
   const int P = plan_passes(num_iters(n), sizes);

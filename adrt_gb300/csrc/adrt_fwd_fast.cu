@@ -214,21 +214,22 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
 // selection of this lane's and the previous lane's 16-byte chunk.  Slot 0 of
 // `raw` holds the chunk that precedes the first one, seeding lane 0.
 template <int A4>
-__device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, float *xs) {
+__device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, float *xs,
+                                             size_t mstride, int cs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
   constexpr int IT = NCH / 32;
   float4 raw[IT + 1][4];
 #pragma unroll
   for (int jj = 0; jj < 4; ++jj) {
     const int j = 4 * mq + jj;
-    const float *row = src + (size_t)(j * 32) * CS;
+    const float *row = src + (size_t)j * mstride;
     const int gb = tbase - 4 * ((ap * j) >> 2);
 #pragma unroll
     for (int it = 0; it <= IT; ++it) {
       // slot 0: the chunk before chunk 0 (only lane 31's copy is used)
       const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
       if (g0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
-      else if (g0 >= CS) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
+      else if (g0 >= cs) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
       else raw[it][jj] = ld4_stream(row + g0);
     }
   }
@@ -361,7 +362,7 @@ __device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, i
 }
 
 template <int L1>
-__device__ __forceinline__ void group2_passB(const float *xs, float *dst_q, int ap, int c0) {
+__device__ __forceinline__ void group2_passB(const float *xs, float *dst_q, int ap, int c0, int n) {
   int b;
   bool active, store;
   group2_lane(b, active, store);
@@ -372,11 +373,11 @@ __device__ __forceinline__ void group2_passB(const float *xs, float *dst_q, int 
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int d = d0 + k;
-    if (d < C) {
+    if (d < 2 * n - 1) {
       float v[8];
 #pragma unroll
       for (int l = 0; l < 8; ++l) v[l] = out[l][k];
-      st8_stream(dst_q + (size_t)d * N + ap * 32 + 8 * L1, v);
+      st8_stream(dst_q + (size_t)d * n + ap * 32 + 8 * L1, v);
     }
   }
 }
@@ -404,49 +405,65 @@ __global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__
   }
 }
 
+// Pass B for any n >= 64: the last five stages.  inter layout per image:
+// [q][g (32)][a (n/32)][cs]; out: (4, 2n-1, n).
 __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__ inter,
-                                                       float *__restrict__ out, int nimg) {
+                                                       float *__restrict__ out, int n, int cs,
+                                                       int col_tiles) {
   extern __shared__ __align__(16) float xs[];
+  const int a_in = n / 32;
   int t = blockIdx.x;
-  const int ct = t % COL_TILES; t /= COL_TILES;
-  const int ap = t % 32; t /= 32;
+  const int ct = t % col_tiles; t /= col_tiles;
+  const int ap = t % a_in; t /= a_in;
   const int q = t % 4; t /= 4;
   const int bimg = t;
   const int c0 = ct * W, tbase = c0 - HALO;
   // member j row: inter[bimg][q][j][ap][*]
-  const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * 32 + ap) * CS;
+  const size_t mstride = (size_t)a_in * cs;
+  const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * a_in + ap) * cs;
   switch (ap & 3) {
-    case 0: group1_passB<0>(src, ap, tbase, xs); break;
-    case 1: group1_passB<1>(src, ap, tbase, xs); break;
-    case 2: group1_passB<2>(src, ap, tbase, xs); break;
-    default: group1_passB<3>(src, ap, tbase, xs); break;
+    case 0: group1_passB<0>(src, ap, tbase, xs, mstride, cs); break;
+    case 1: group1_passB<1>(src, ap, tbase, xs, mstride, cs); break;
+    case 2: group1_passB<2>(src, ap, tbase, xs, mstride, cs); break;
+    default: group1_passB<3>(src, ap, tbase, xs, mstride, cs); break;
   }
   __syncthreads();
-  float *dst_q = out + (size_t)(bimg * 4 + q) * C * N;
+  float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
   switch ((threadIdx.x >> 5) & 3) {
-    case 0: group2_passB<0>(xs, dst_q, ap, c0); break;
-    case 1: group2_passB<1>(xs, dst_q, ap, c0); break;
-    case 2: group2_passB<2>(xs, dst_q, ap, c0); break;
-    default: group2_passB<3>(xs, dst_q, ap, c0); break;
+    case 0: group2_passB<0>(xs, dst_q, ap, c0, n); break;
+    case 1: group2_passB<1>(xs, dst_q, ap, c0, n); break;
+    case 2: group2_passB<2>(xs, dst_q, ap, c0, n); break;
+    default: group2_passB<3>(xs, dst_q, ap, c0, n); break;
   }
 }
 
 }  // namespace fast
 
-// Bytes of intermediate per image for the fast path.
-size_t fast_inter_bytes() { return sizeof(float) * 4 * 32 * 32 * fast::CS; }
+// Row stride of the fast path's intermediate: 2n-1 offsets rounded up to a
+// multiple of 8 floats (32 bytes) so every row start is 256-bit aligned.
+static int fast_cs(i64 n) { return (int)(((2 * n - 1) + 7) / 8 * 8); }
 
-bool fast_forward_eligible(i64 n, size_t elem) { return n == fast::N && elem == 4; }
+// Bytes of intermediate per image: [q][32][n/32][cs] float32.
+size_t fast_inter_bytes(i64 n) { return sizeof(float) * 4 * (size_t)n * fast_cs(n); }
 
-// Images per chunk so that the intermediate (33.5 MB per image) stays in L2.
-static i64 fast_chunk(i64 batch) {
-  const i64 k = 2;
+bool fast_forward_eligible(i64 n, size_t elem) { return elem == 4 && n >= 64 && n <= fast::N; }
+
+// Images per chunk so that the chunk's intermediate stays in L2 (~48 MB).
+static i64 fast_chunk(i64 batch, i64 n) {
+  i64 k = (i64)((size_t)(48u << 20) / fast_inter_bytes(n));
+  if (k < 1) k = 1;
+  if (n == fast::N) k = 2;
   return batch < k ? batch : k;
 }
 
-size_t fast_workspace_bytes(i64 batch) { return fast_inter_bytes() * (size_t)fast_chunk(batch); }
+size_t fast_workspace_bytes(i64 batch, i64 n) { return fast_inter_bytes(n) * (size_t)fast_chunk(batch, n); }
 
-int adrt_forward_fast(const float *in, float *out, i64 batch, void *ws, size_t ws_bytes,
+// First pass for n < 1024: the generic kernel runs stages 0..L-6 and writes
+// the padded intermediate (adrt_fwd.cu).
+int fwd_first_pass_padded(const float *in, float *inter, i64 batch, i64 n, int stages, int cs,
+                          cudaStream_t st);
+
+int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                       cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
@@ -454,18 +471,28 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, void *ws, size_t w
     cudaFuncSetAttribute(fast::pass_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
     configured = true;
   }
-  const i64 per = (i64)fast_inter_bytes();
-  i64 chunk = fast_chunk(batch);
+  const i64 per = (i64)fast_inter_bytes(n);
+  i64 chunk = fast_chunk(batch, n);
   if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
   if ((i64)ws_bytes < per * chunk) chunk = (i64)ws_bytes / per;
   float *inter = static_cast<float *>(ws);
+  const int cs = fast_cs(n);
+  const int col_tiles = (int)((2 * n - 1 + fast::W - 1) / fast::W);
+  const int L = num_iters(n);
   for (i64 b0 = 0; b0 < batch; b0 += chunk) {
     const int nb = (int)((batch - b0) < chunk ? (batch - b0) : chunk);
-    const unsigned grid = (unsigned)(nb * 4 * 32 * fast::COL_TILES);
-    fast::pass_a_kernel<<<grid, fast::NT, fast::SMEM, st>>>(in + b0 * fast::N * fast::N, inter, nb);
-    int rc = launch_status();
+    int rc;
+    if (n == fast::N) {
+      const unsigned grid = (unsigned)(nb * 4 * 32 * fast::COL_TILES);
+      fast::pass_a_kernel<<<grid, fast::NT, fast::SMEM, st>>>(in + b0 * n * n, inter, nb);
+      rc = launch_status();
+    } else {
+      rc = fwd_first_pass_padded(in + b0 * n * n, inter, nb, n, L - 5, cs, st);
+    }
     if (rc) return rc;
-    fast::pass_b_kernel<<<grid, fast::NT, fast::SMEM, st>>>(inter, out + b0 * 4 * (i64)fast::C * fast::N, nb);
+    const unsigned gridb = (unsigned)(nb * 4 * (n / 32) * col_tiles);
+    fast::pass_b_kernel<<<gridb, fast::NT, fast::SMEM, st>>>(inter, out + b0 * 4 * (2 * n - 1) * n, (int)n, cs,
+                                                             col_tiles);
     rc = launch_status();
     if (rc) return rc;
   }

@@ -37,14 +37,26 @@ struct BwdPassArgs {
 // Buffer layout between passes, per (b, q): [angle s][section p][offset c],
 // the reference's bdrt buffer.  After forward stage k0 there are A = 2^k0
 // angles and R = n / 2^k0 sections.
+// Shared-memory rows of one tile (same thread mapping as the forward kernel);
+// a 32-element tail pad keeps the right-shifted reads of the last row in bounds.
+template <int ROWS>
+struct BwdTile {
+  static constexpr int TWP = kBwdW + kBwdHalo;
+  static constexpr int LPR = kBwdThreads / ROWS;
+  static constexpr int RPW = LPR >= 32 ? 1 : 32 / LPR;
+  static constexpr int RS = TWP + (RPW > 1 ? 32 / RPW : 0);
+  static constexpr int BUF = ROWS * RS + 32;
+};
+
 template <typename T, int S, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kBwdThreads)
 bwd_pass_kernel(BwdPassArgs args) {
   constexpr int ROWS = 1 << S;
-  constexpr int TWP = kBwdW + kBwdHalo;
+  using TL = BwdTile<ROWS>;
+  constexpr int TWP = TL::TWP, RS = TL::RS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf0 = reinterpret_cast<T *>(smem_raw);
-  T *buf1 = buf0 + ROWS * TWP;
+  T *buf1 = buf0 + TL::BUF;
 
   const i64 n = args.n;
   const i64 C = 2 * n - 1;
@@ -76,7 +88,7 @@ bwd_pass_kernel(BwdPassArgs args) {
       const i64 c = c0 + u;
       T v = T(0);
       if (c < C) v = src[c * n + ap * ROWS + l];
-      buf0[l * TWP + u] = v;
+      buf0[l * RS + u] = v;
     }
   } else {
     const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * A_hi * R_hi * C;
@@ -85,7 +97,7 @@ bwd_pass_kernel(BwdPassArgs args) {
       const i64 c = c0 + u;
       T v = T(0);
       if (c < C) v = src[((ap * ROWS + l) * R_hi + r) * C + c];
-      buf0[l * TWP + u] = v;
+      buf0[l * RS + u] = v;
     }
   }
   __syncthreads();
@@ -94,29 +106,30 @@ bwd_pass_kernel(BwdPassArgs args) {
   // Level j+1 buffer rows: combo m, local angle la -> row m * 2^(j+1) + la.
   // Level j buffer rows:   combo m', local angle li -> row m' * 2^j + li.
   T *cur = buf0, *nxt = buf1;
+  const int rowo = threadIdx.x / TL::LPR, lr = threadIdx.x % TL::LPR;
 #pragma unroll
   for (int j = S - 1; j >= 0; --j) {
     const int Al_hi = 2 << j;          // local angles at level j+1
     const int Al_lo = 1 << j;          // local angles at level j
-    const int Rl_lo = ROWS >> j;       // combos at level j
-    for (int idx = threadIdx.x; idx < Rl_lo * Al_lo * TWP; idx += blockDim.x) {
-      const int u = idx % TWP;
-      const int row = idx / TWP;
-      const int mm = row / Al_lo, li = row % Al_lo;  // level-j combo, angle
-      const int m = mm >> 1;                         // parent combo at level j+1
-      const T *ya = cur + (m * Al_hi + 2 * li) * TWP;
-      const T *yb = ya + TWP;
-      T v;
-      if ((mm & 1) == 0) {
-        v = add_rn(ya[u], yb[u]);  // left (garbage beyond the buffer is never used)
-      } else {
-        // Reference offset of ya's operand: tile position u+li, parent mapping a'*2m*2^j.
-        const i64 ref_la = c0 + u + li - ap * (i64)((2 * m) << j);
-        if (u + li + 1 < TWP && ref_la + 1 <= C - 1) v = add_rn(ya[u + li], yb[u + li + 1]);
-        else if (ref_la == C - 1 && u + li < TWP) v = ya[u + li];
+    const int mm = rowo / Al_lo, li = rowo % Al_lo;  // level-j combo, angle
+    const int m = mm >> 1;                           // parent combo at level j+1
+    const T *ya = cur + (m * Al_hi + 2 * li) * RS;
+    const T *yb = ya + RS;
+    T *np = nxt + rowo * RS;
+    if ((mm & 1) == 0) {
+      // left: la + lb (positions past the buffer end are never used)
+      for (int u = lr; u < TWP; u += TL::LPR) np[u] = add_rn(ya[u], yb[u]);
+    } else {
+      // right: reference offset of la is base + u, with the parent mapping a'*2m*2^j.
+      const i64 base = c0 + li - ap * (i64)((2 * m) << j);
+      const i64 last_add = C - 2 - base;  // u <= last_add: la + lbb
+      for (int u = lr; u < TWP; u += TL::LPR) {
+        T v;
+        if (u <= last_add) v = add_rn(ya[u + li], yb[u + li + 1]);
+        else if (u == last_add + 1) v = ya[u + li];  // copy of la at offset C-1
         else v = T(0);
+        np[u] = v;
       }
-      nxt[row * TWP + u] = v;
     }
     __syncthreads();
     T *tmp = cur; cur = nxt; nxt = tmp;
@@ -129,14 +142,14 @@ bwd_pass_kernel(BwdPassArgs args) {
     for (int idx = threadIdx.x; idx < kBwdW * ROWS; idx += blockDim.x) {
       const int i = idx % ROWS, w = idx / ROWS;
       const i64 c = c0 + w;
-      if (c < C) st_stream(&dst[c * n + r * ROWS + i], cur[i * TWP + w]);
+      if (c < C) st_stream(&dst[c * n + r * ROWS + i], cur[i * RS + w]);
     }
   } else {
     T *dst = static_cast<T *>(args.out) + (b * 4 + q) * A_lo * R_lo * C;
     for (int idx = threadIdx.x; idx < ROWS * kBwdW; idx += blockDim.x) {
       const int i = idx / kBwdW, w = idx % kBwdW;
       const i64 c = c0 + w - ap * i;
-      if (c >= 0 && c < C) dst[(ap * R_lo + r * ROWS + i) * C + c] = cur[i * TWP + w];
+      if (c >= 0 && c < C) dst[(ap * R_lo + r * ROWS + i) * C + c] = cur[i * RS + w];
     }
   }
 }
@@ -151,7 +164,7 @@ static int plan_passes_bwd(int L, int *sizes) {
 template <typename T, int S, bool FIRST, bool LAST>
 static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S;
-  const size_t smem = 2 * sizeof(T) * ROWS * (kBwdW + kBwdHalo);
+  const size_t smem = 2 * sizeof(T) * BwdTile<ROWS>::BUF;
   auto kern = bwd_pass_kernel<T, S, FIRST, LAST>;
   static bool configured = false;
   if (!configured) {

@@ -281,7 +281,10 @@ def main():
     e2e = None
     if args.e2e_steps > 0:
         xh = x.cpu().pin_memory()
-        yh = adrt.adrt(xh)
+        # Two untimed calls: the result of one call is alive while the next
+        # one runs, so the pinned-memory cache settles on two result buffers.
+        for _ in range(2):
+            yh = adrt.adrt(xh)
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
