@@ -64,6 +64,10 @@ SIGNATURES = {
     "adrt_gb300_sumsq_workspace_size": [],
     "adrt_gb300_sumsq": [_v, _i64, _int, _v, _v, _v],
     "adrt_gb300_cg_workspace_size": [_i64],
+    "adrt_gb300_ragged_workspace_size": [_v, _i64, _int, ctypes.POINTER(_sz)],
+    "adrt_gb300_adrt_ragged": [_v, _v, _v, _i64, _int, _v, _sz, _v],
+    "adrt_gb300_adrt_ragged_ex": [_v, _v, _v, _i64, _int, _v, _sz, ctypes.c_uint64, _i64, _v],
+    "adrt_gb300_ragged_status": [_v, _v, _i64, _int, _v],
     "adrt_gb300_batched_dot": [_v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],

@@ -21,6 +21,9 @@
 // are fused into its load); the last pass writes the (4, 2n-1, n) layout
 // directly (the transpose is fused into its store).  Passes in between use a
 // workspace laid out like the reference's buffer: [b][q][R][A][2n-1].
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 
 namespace adrtg {
@@ -50,13 +53,19 @@ struct FwdTile {
   static constexpr int BUF = ROWS * RS;
 };
 
+// Loads for non-first passes go through L2 only (the ragged kernel reads
+// intermediates written by other CTAs of the same launch).
+template <typename T>
+__device__ __forceinline__ T ld_l2(const T *p) { return __ldcg(p); }
+
+// One tile of one pass.  `tile` enumerates (b, q, r, a', column tile), column
+// tile fastest; `smem_raw` holds two tile buffers.
 template <typename T, int S, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kFwdThreads)
-fwd_pass_kernel(FwdPassArgs args) {
+__device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
+                                         unsigned char *smem_raw) {
   constexpr int ROWS = 1 << S;
   using TL = FwdTile<ROWS>;
   constexpr int TWP = TL::TWP, RS = TL::RS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf0 = reinterpret_cast<T *>(smem_raw);
   T *buf1 = buf0 + TL::BUF;
 
@@ -70,7 +79,7 @@ fwd_pass_kernel(FwdPassArgs args) {
   const int col_tiles = (int)((C + kFwdW - 1) / kFwdW);
 
   // Decode the tile: (b, q, r, a', column tile), column tile fastest.
-  i64 t = blockIdx.x;
+  i64 t = tile;
   const int ct = (int)(t % col_tiles); t /= col_tiles;
   const i64 ap = t % A_in; t /= A_in;
   const i64 r = t % R_out; t /= R_out;
@@ -111,7 +120,7 @@ fwd_pass_kernel(FwdPassArgs args) {
       const i64 ref = tbase + u - ap * i;
       const i64 row = (r * ROWS + i) * A_in + ap;
       T v = ref < 0 ? T(-0.0) : T(0);
-      if (ref >= 0 && ref < C) v = src[row * C + ref];
+      if (ref >= 0 && ref < C) v = ld_l2(&src[row * C + ref]);
       buf0[i * RS + u] = v;
     }
   }
@@ -152,6 +161,19 @@ fwd_pass_kernel(FwdPassArgs args) {
       if (c < C) dst[(r * A_out + ap * ROWS + l) * cs + c] = cur[l * RS + kFwdHalo + w];
     }
   }
+}
+
+template <typename T, int S, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kFwdThreads)
+fwd_pass_kernel(FwdPassArgs args) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fwd_tile<T, S, FIRST, LAST>(args, blockIdx.x, smem_raw);
+}
+
+// Tiles in one pass of one image.
+static __host__ __device__ i64 fwd_pass_tiles(i64 n, int S) {
+  const i64 C = 2 * n - 1;
+  return 4 * (n >> S) * ((C + kFwdW - 1) / kFwdW);
 }
 
 // ---- host side --------------------------------------------------------------
@@ -269,5 +291,239 @@ int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
 
 template int adrt_forward<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t);
 template int adrt_forward<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t);
+
+
+
+// ---------------------------------------------------------------------------
+// Ragged batches: images of different power-of-two sizes in one persistent
+// launch.  CTAs take tickets from a device queue of (image, pass, tile) items
+// (all first-pass items, largest images first, then all second-pass items).
+// A second-pass item waits until every first-pass tile of its image has been
+// counted.  Every item a waiting CTA depends on has a smaller ticket and is
+// held by a CTA that is already running and never waits itself, so the waits
+// always end; each wait is still bounded (by %globaltimer), and on expiry the
+// kernel raises the error word and stops taking work.
+// ---------------------------------------------------------------------------
+
+struct RaggedImage {
+  i64 in_off, out_off, inter_off;  // element offsets in the packed buffers
+  int n, s0, s1;                   // side, stages of pass 0 and pass 1 (0: none)
+  int tiles0;                      // tiles of pass 0
+};
+
+struct RaggedItem {
+  int image, pass, tile, pad;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <typename T, bool FIRST, bool LAST>
+__device__ __forceinline__ void ragged_tile_S(int S, const FwdPassArgs &a, i64 tile,
+                                              unsigned char *smem) {
+  switch (S) {
+    case 0: fwd_tile<T, 0, FIRST, LAST>(a, tile, smem); break;
+    case 1: fwd_tile<T, 1, FIRST, LAST>(a, tile, smem); break;
+    case 2: fwd_tile<T, 2, FIRST, LAST>(a, tile, smem); break;
+    case 3: fwd_tile<T, 3, FIRST, LAST>(a, tile, smem); break;
+    case 4: fwd_tile<T, 4, FIRST, LAST>(a, tile, smem); break;
+    default: fwd_tile<T, 5, FIRST, LAST>(a, tile, smem); break;
+  }
+}
+
+// ctl[0]: next ticket, ctl[1]: error word.
+template <typename T>
+__global__ void __launch_bounds__(kFwdThreads)
+ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__ inter,
+                  const RaggedImage *__restrict__ imgs, const RaggedItem *__restrict__ items,
+                  int n_items, unsigned *ctl, unsigned *counters, unsigned long long wait_ns) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ int s_ok;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(&ctl[0], 1u);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const RaggedItem item = items[it];
+    const RaggedImage im = imgs[item.image];
+    if (item.pass == 1) {
+      if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        while (atomicAdd(&counters[item.image], 0u) < (unsigned)im.tiles0) {
+          if (atomicAdd(&ctl[1], 0u) != 0u || global_ns() - t0 > wait_ns) {
+            ok = 0;
+            atomicExch(&ctl[1], 1u);
+            break;
+          }
+          __nanosleep(128);
+        }
+        __threadfence();
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (!s_ok) break;
+    }
+    FwdPassArgs a;
+    a.n = im.n;
+    a.batch = 1;
+    a.cs_out = 0;
+    if (item.pass == 0) {
+      a.in = in + im.in_off;
+      a.k0 = 0;
+      if (im.s1 == 0) {
+        a.out = out + im.out_off;
+        ragged_tile_S<T, true, true>(im.s0, a, item.tile, smem_raw);
+      } else {
+        a.out = inter + im.inter_off;
+        ragged_tile_S<T, true, false>(im.s0, a, item.tile, smem_raw);
+      }
+    } else {
+      a.in = inter + im.inter_off;
+      a.out = out + im.out_off;
+      a.k0 = im.s0;
+      ragged_tile_S<T, false, true>(im.s1, a, item.tile, smem_raw);
+    }
+    __syncthreads();
+    if (item.pass == 0 && im.s1 > 0 && threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(&counters[item.image], 1u);
+    }
+  }
+}
+
+// Workspace: [images][items][ctl x2 + counters][intermediates], each part
+// 256-byte aligned.
+struct RaggedPlan {
+  size_t off_imgs, off_items, off_ctl, off_inter, total;
+  i64 n_items, inter_elems;
+};
+
+static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+static int ragged_plan(const int64_t *sizes, i64 count, size_t elem, RaggedPlan &p) {
+  i64 items = 0, inter = 0;
+  for (i64 i = 0; i < count; ++i) {
+    const i64 n = sizes[i];
+    if (n < 1 || !is_pow2(n) || n > 1024) return ADRT_GB300_ERR_SHAPE;
+    const int L = num_iters(n);
+    int sz[16];
+    const int P = plan_passes(L, sz);
+    items += fwd_pass_tiles(n, sz[0]);
+    if (P == 2) {
+      items += fwd_pass_tiles(n, sz[1]);
+      inter += 4 * n * (2 * n - 1);
+    }
+  }
+  p.n_items = items;
+  p.inter_elems = inter;
+  p.off_imgs = 0;
+  p.off_items = align256(sizeof(RaggedImage) * (size_t)count);
+  p.off_ctl = p.off_items + align256(sizeof(RaggedItem) * (size_t)items);
+  p.off_inter = p.off_ctl + align256(sizeof(unsigned) * (size_t)(2 + count));
+  p.total = p.off_inter + align256(elem * (size_t)inter);
+  return ADRT_GB300_OK;
+}
+
+size_t ragged_workspace_bytes(const int64_t *sizes, i64 count, size_t elem, int *rc) {
+  RaggedPlan p;
+  *rc = ragged_plan(sizes, count, elem, p);
+  return *rc ? 0 : p.total;
+}
+
+// Wall-clock bound on one wait (the whole batch runs in far less).
+constexpr unsigned long long kRaggedWaitNs = 4000000000ull;
+
+template <typename T>
+int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, size_t ws_bytes,
+                unsigned long long wait_ns, i64 starve_image, cudaStream_t st) {
+  RaggedPlan p;
+  int rc = ragged_plan(sizes, count, sizeof(T), p);
+  if (rc) return rc;
+  if (ws == nullptr || ws_bytes < p.total) return ADRT_GB300_ERR_WORKSPACE;
+  if (p.n_items > 0x7fffffff) return ADRT_GB300_ERR_TOO_LARGE;
+  // Host-side descriptors.
+  std::vector<RaggedImage> imgs((size_t)count);
+  i64 in_off = 0, out_off = 0, inter_off = 0;
+  for (i64 i = 0; i < count; ++i) {
+    const i64 n = sizes[i];
+    int sz[16];
+    const int P = plan_passes(num_iters(n), sz);
+    RaggedImage &im = imgs[(size_t)i];
+    im.in_off = in_off;
+    im.out_off = out_off;
+    im.inter_off = inter_off;
+    im.n = (int)n;
+    im.s0 = sz[0];
+    im.s1 = P == 2 ? sz[1] : 0;
+    im.tiles0 = (int)fwd_pass_tiles(n, im.s0);
+    // Fault injection for tests: the image's second pass waits for one more
+    // first-pass tile than exists, so its wait can only expire.
+    if (i == starve_image && im.s1 > 0) im.tiles0 += 1;
+    in_off += n * n;
+    out_off += 4 * n * (2 * n - 1);
+    if (P == 2) inter_off += 4 * n * (2 * n - 1);
+  }
+  // Items: first passes (largest images first), then second passes.
+  std::vector<i64> order((size_t)count);
+  for (i64 i = 0; i < count; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](i64 a, i64 b) { return sizes[a] > sizes[b]; });
+  std::vector<RaggedItem> items;
+  items.reserve((size_t)p.n_items);
+  for (int pass = 0; pass < 2; ++pass)
+    for (i64 oi : order) {
+      const RaggedImage &im = imgs[(size_t)oi];
+      const int S = pass == 0 ? im.s0 : im.s1;
+      if (pass == 1 && im.s1 == 0) continue;
+      const i64 nt = fwd_pass_tiles(im.n, S);
+      for (i64 t = 0; t < nt; ++t) items.push_back(RaggedItem{(int)oi, pass, (int)t, 0});
+    }
+  char *base = static_cast<char *>(ws);
+  if (cudaMemcpyAsync(base + p.off_imgs, imgs.data(), sizeof(RaggedImage) * imgs.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(base + p.off_items, items.data(), sizeof(RaggedItem) * items.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(base + p.off_ctl, 0, sizeof(unsigned) * (size_t)(2 + count), st) != cudaSuccess)
+    return ADRT_GB300_ERR_CUDA;
+  // The copies above are from pageable memory: they complete before the calls return.
+  constexpr size_t smem = 2 * sizeof(T) * FwdTile<32>::BUF;
+  auto kern = ragged_fwd_kernel<T>;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFwdThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  i64 grid = (i64)sms * per_sm;
+  if (grid > p.n_items) grid = p.n_items;
+  if (grid < 1) return ADRT_GB300_OK;
+  unsigned *ctl = reinterpret_cast<unsigned *>(base + p.off_ctl);
+  kern<<<(unsigned)grid, kFwdThreads, smem, st>>>(
+      in, out, reinterpret_cast<T *>(base + p.off_inter),
+      reinterpret_cast<const RaggedImage *>(base + p.off_imgs),
+      reinterpret_cast<const RaggedItem *>(base + p.off_items), (int)p.n_items, ctl, ctl + 2,
+      wait_ns ? wait_ns : kRaggedWaitNs);
+  return launch_status();
+}
+
+template int adrt_ragged<float>(const float *, float *, const int64_t *, i64, void *, size_t,
+                                unsigned long long, i64, cudaStream_t);
+template int adrt_ragged<double>(const double *, double *, const int64_t *, i64, void *, size_t,
+                                 unsigned long long, i64, cudaStream_t);
+
+// Byte offset of the error word in the workspace of a ragged call.
+size_t ragged_error_offset(const int64_t *sizes, i64 count, size_t elem) {
+  RaggedPlan p;
+  if (ragged_plan(sizes, count, elem, p)) return 0;
+  return p.off_ctl + sizeof(unsigned);
+}
 
 }  // namespace adrtg

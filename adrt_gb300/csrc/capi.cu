@@ -17,6 +17,10 @@ template <typename T> int fmg_correction_launch(const T *, T *, i64, i64, cudaSt
 template <typename T> int binary_launch(const T *, const T *, T *, i64, int, cudaStream_t);
 template <typename T> int sumsq_launch(const T *, i64, double *, void *, cudaStream_t);
 size_t sumsq_workspace_bytes();
+size_t ragged_workspace_bytes(const int64_t *, i64, size_t, int *);
+size_t ragged_error_offset(const int64_t *, i64, size_t);
+template <typename T>
+int adrt_ragged(const T *, T *, const int64_t *, i64, void *, size_t, unsigned long long, i64, cudaStream_t);
 size_t cg_workspace_bytes(i64);
 template <typename T> int batched_dot_launch(const T *, const T *, double *, i64, i64, void *, cudaStream_t);
 template <typename T>
@@ -308,6 +312,54 @@ int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double
   return DISPATCH(dtype,
                   cg_direction_launch<float>((float *)p, (const float *)r, rs_new, rs, active, batch, per, S(stream)),
                   cg_direction_launch<double>((double *)p, (const double *)r, rs_new, rs, active, batch, per, S(stream)));
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int adrt_gb300_ragged_workspace_size(const int64_t *sizes, int64_t count, int dtype, size_t *bytes) {
+  int rc;
+  if (!sizes || !bytes) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (count < 1) return ADRT_GB300_ERR_SHAPE;
+  *bytes = ragged_workspace_bytes(sizes, count, dtype_size(dtype), &rc);
+  return rc;
+}
+
+int adrt_gb300_adrt_ragged_ex(const void *in, void *out, const int64_t *sizes, int64_t count,
+                              int dtype, void *ws, size_t ws_bytes, uint64_t wait_ns,
+                              int64_t starve_image, void *stream) {
+  int rc;
+  if (!in || !out || !sizes) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (count < 1) return ADRT_GB300_ERR_SHAPE;
+  return DISPATCH(dtype,
+                  adrt_ragged<float>((const float *)in, (float *)out, sizes, count, ws, ws_bytes, wait_ns,
+                                     starve_image, S(stream)),
+                  adrt_ragged<double>((const double *)in, (double *)out, sizes, count, ws, ws_bytes, wait_ns,
+                                      starve_image, S(stream)));
+}
+
+int adrt_gb300_adrt_ragged(const void *in, void *out, const int64_t *sizes, int64_t count, int dtype,
+                           void *ws, size_t ws_bytes, void *stream) {
+  return adrt_gb300_adrt_ragged_ex(in, out, sizes, count, dtype, ws, ws_bytes, 0, -1, stream);
+}
+
+int adrt_gb300_ragged_status(const void *ws, const int64_t *sizes, int64_t count, int dtype,
+                             void *stream) {
+  int rc;
+  if (!ws || !sizes) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (count < 1) return ADRT_GB300_ERR_SHAPE;
+  const size_t off = ragged_error_offset(sizes, count, dtype_size(dtype));
+  if (off == 0) return ADRT_GB300_ERR_SHAPE;
+  unsigned word = 0;
+  if (cudaMemcpyAsync(&word, static_cast<const char *>(ws) + off, sizeof(word), cudaMemcpyDeviceToHost,
+                      S(stream)) != cudaSuccess ||
+      cudaStreamSynchronize(S(stream)) != cudaSuccess)
+    return ADRT_GB300_ERR_CUDA;
+  return word ? ADRT_GB300_ERR_TIMEOUT : ADRT_GB300_OK;
 }
 
 }  // extern "C"

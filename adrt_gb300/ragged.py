@@ -1,0 +1,93 @@
+"""Ragged batches: images of different power-of-two sizes.
+
+``adrt_ragged(images)`` transforms a list of square images (sides 1..1024,
+one dtype, one CUDA device) in a single persistent kernel launch that takes
+(image, pass, tile) work items from a device-side queue; each result equals
+``adrt_gb300.adrt`` of that image bit for bit.  ``iadrt_ragged`` and
+``iadrt_fmg_ragged`` invert such a list (grouped by size, resp. image by image,
+as the reference's ``iadrt_fmg`` takes no batch).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections import defaultdict
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._ops import iadrt as _iadrt
+from ._wrappers import float_code, is_pow2
+
+__all__ = ["adrt_ragged", "iadrt_ragged", "iadrt_fmg_ragged"]
+
+
+def _sizes_array(images):
+    if not isinstance(images, (list, tuple)) or not images:
+        raise TypeError("images must be a non-empty list of CUDA tensors")
+    dt, dev = images[0].dtype, images[0].device
+    sizes = []
+    for im in images:
+        if not (isinstance(im, torch.Tensor) and im.is_cuda):
+            raise TypeError("images must be CUDA tensors")
+        if im.ndim != 2 or im.shape[0] != im.shape[1] or not is_pow2(int(im.shape[0])):
+            raise ValueError("each image must be square with a power of two shape")
+        if im.shape[0] > 1024:
+            raise ValueError("ragged batches take sides up to 1024")
+        if im.dtype != dt or im.device != dev:
+            raise ValueError("all images must share dtype and device")
+        sizes.append(int(im.shape[0]))
+    return np.asarray(sizes, dtype=np.int64), dt, dev
+
+
+def _launch(images, wait_ns=0, starve_image=-1):
+    sizes, dt, dev = _sizes_array(images)
+    code = float_code(images[0])
+    lib = _lib.load()
+    sp = sizes.ctypes.data_as(ctypes.c_void_p)
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.adrt_gb300_ragged_workspace_size(sp, len(sizes), code, ctypes.byref(nbytes)), "ragged")
+    ws = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=dev)
+    packed = torch.cat([im.contiguous().reshape(-1) for im in images])
+    outn = [4 * n * (2 * n - 1) for n in sizes]
+    out = torch.empty(sum(outn), dtype=dt, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    rc = lib.adrt_gb300_adrt_ragged_ex(packed.data_ptr(), out.data_ptr(), sp, len(sizes), code,
+                                       ws.data_ptr(), nbytes.value, wait_ns, starve_image, stream)
+    _lib.check(rc, "adrt_ragged")
+    status = lib.adrt_gb300_ragged_status(ws.data_ptr(), sp, len(sizes), code, stream)
+    views, off = [], 0
+    for n, k in zip(sizes, outn):
+        views.append(out[off:off + k].view(4, 2 * int(n) - 1, int(n)))
+        off += k
+    return views, status
+
+
+def adrt_ragged(images):
+    """Forward ADRT of each image of a ragged list, in one persistent launch.
+
+    Raises RuntimeError if a device-side wait of the launch expired."""
+    views, status = _launch(images)
+    _lib.check(status, "adrt_ragged")
+    return views
+
+
+def iadrt_ragged(arrays):
+    """Exact inverse of each (4, 2n-1, n) array; arrays of one size run as a batch."""
+    groups = defaultdict(list)
+    for i, a in enumerate(arrays):
+        groups[int(a.shape[-1])].append(i)
+    out = [None] * len(arrays)
+    for n, idx in groups.items():
+        res = _iadrt(torch.stack([arrays[i] for i in idx]))
+        for k, i in enumerate(idx):
+            out[i] = res[k]
+    return out
+
+
+def iadrt_fmg_ragged(arrays, max_iters=None):
+    """Full-multigrid inverse of each array (the reference's iadrt_fmg takes no batch)."""
+    from . import iadrt_fmg
+
+    return [iadrt_fmg(a, max_iters=max_iters) for a in arrays]

@@ -90,6 +90,28 @@ int adrt_gb300_adrt(const void *in, void *out, int64_t batch, int64_t n, int dty
 int adrt_gb300_adrt_noalloc(const void *in, void *out, int64_t batch, int64_t n, int dtype,
                             void *stream);
 
+/* ---- Ragged batches: `count` square images of power-of-two sides sizes[i]
+ * (1 <= n <= 1024), packed back to back in `in` (image i after images 0..i-1),
+ * transformed in one persistent launch into `out`, packed the same way
+ * ((4, 2n-1, n) per image).  No counterpart in the reference, which
+ * transforms one size per call; each image's result equals adrt_gb300_adrt's.
+ * CTAs take (image, pass, tile) items from a device-side queue; second-pass
+ * items wait, with a bounded device-side wait, for their image's first pass.
+ * After the call, adrt_gb300_ragged_status synchronises the stream and
+ * reports ADRT_GB300_ERR_TIMEOUT if any wait expired. */
+int adrt_gb300_ragged_workspace_size(const int64_t *sizes, int64_t count, int dtype, size_t *bytes);
+int adrt_gb300_adrt_ragged(const void *in, void *out, const int64_t *sizes, int64_t count, int dtype,
+                           void *workspace, size_t workspace_bytes, void *stream);
+int adrt_gb300_ragged_status(const void *workspace, const int64_t *sizes, int64_t count, int dtype,
+                             void *stream);
+/* As adrt_gb300_adrt_ragged with the wait limit in nanoseconds (0: default,
+ * 4 s) and, for failure-detection tests, starve_image >= 0: that image's
+ * second pass waits for a first-pass tile that does not exist, so its wait
+ * expires and the status reports ADRT_GB300_ERR_TIMEOUT. */
+int adrt_gb300_adrt_ragged_ex(const void *in, void *out, const int64_t *sizes, int64_t count,
+                              int dtype, void *workspace, size_t workspace_bytes, uint64_t wait_ns,
+                              int64_t starve_image, void *stream);
+
 /* One forward stage in the output layout: (batch, 4, 2n-1, n) -> same.
  * Replaces adrt::adrt_step (src/adrt/adrt_cdefs_adrt.hpp:215-258),
  * bound as _adrt_cdefs.adrt_step (src/adrt/adrt_cdefs_py.cpp:343-412). */
