@@ -17,6 +17,7 @@ template <typename T> int fmg_correction_launch(const T *, T *, i64, i64, cudaSt
 template <typename T> int binary_launch(const T *, const T *, T *, i64, int, cudaStream_t);
 template <typename T> int sumsq_launch(const T *, i64, double *, void *, cudaStream_t);
 size_t sumsq_workspace_bytes();
+unsigned *fast_error_word();
 size_t ragged_workspace_bytes(const int64_t *, i64, size_t, int *);
 size_t ragged_error_offset(const int64_t *, i64, size_t);
 template <typename T>
@@ -363,3 +364,21 @@ int adrt_gb300_ragged_status(const void *ws, const int64_t *sizes, int64_t count
 }
 
 }  // extern "C"
+
+extern "C" int adrt_gb300_device_status(void *stream) {
+  unsigned *w = fast_error_word();
+  if (!w) return ADRT_GB300_ERR_CUDA;
+  unsigned word = 0;
+  cudaStream_t st = S(stream);
+  if (cudaMemcpyAsync(&word, w, sizeof(word), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return ADRT_GB300_ERR_CUDA;
+  if (word) {
+    const unsigned zero = 0;
+    if (cudaMemcpyAsync(w, &zero, sizeof(zero), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return ADRT_GB300_ERR_CUDA;
+    return ADRT_GB300_ERR_TIMEOUT;
+  }
+  return ADRT_GB300_OK;
+}

@@ -65,6 +65,12 @@ int adrt_gb300_num_iters(int64_t n);
  * loaded (all threads, all devices).  For accounting; no reference counterpart. */
 uint64_t adrt_gb300_launch_count(void);
 
+/* Synchronises `stream`, then reports ADRT_GB300_ERR_TIMEOUT (and clears the
+ * condition) if a kernel of this library on the current device gave up a
+ * bounded wait for its bulk copies since the last call; ADRT_GB300_OK
+ * otherwise.  No reference counterpart. */
+int adrt_gb300_device_status(void *stream);
+
 /* Bytes of workspace that `op` needs for `batch` arrays of side n.  May be 0.
  * The reference allocates this temporary itself with PyMem_Malloc
  * (src/adrt/adrt_cdefs_py.cpp:301-307). */

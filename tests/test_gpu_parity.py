@@ -175,3 +175,14 @@ def test_nan_inf_positions(oracle_mod):
     x[1, 10, 10] = np.inf
     x[1, 11, 12] = -np.inf
     assert bits_equal(host(adrt.adrt(dev(x))), oracle_mod.adrt(x))
+
+
+def test_device_status_clean_after_fast_path():
+    from adrt_gb300 import _lib
+
+    x = torch.rand((3, 1024, 1024), device="cuda")
+    adrt.adrt(x)
+    for n in (64, 256, 512):
+        adrt.adrt(torch.rand((2, n, n), device="cuda"))
+    rc = _lib.load().adrt_gb300_device_status(torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.OK
