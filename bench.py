@@ -161,6 +161,40 @@ def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
     }
 
 
+def cg_bench(torch, dev, n=256, batch=512, oracle_batch=32, tol=1e-4):
+    """Plain batched CG on the normal equations for noisy 256 x 256 phantoms:
+    solves/s to ||A^T(Ax-b)|| / ||A^T b|| <= tol, plus the data residual and
+    the error against a float64 CG solution of the same systems."""
+    import adrt_gb300 as adrt
+    from adrt_gb300 import cg as cgmod
+    from adrt_gb300.data import ellipse_phantoms
+
+    xt = ellipse_phantoms(batch, n, seed=900_000, device=dev)
+    b = adrt.adrt(xt)
+    sigma = 1e-3 * b.abs().amax(dim=(1, 2, 3), keepdim=True)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4242)
+    b = b + sigma * torch.randn(b.shape, generator=g, device=dev)
+    cgmod.cg(b[:8], tol=tol, max_iters=200, graph=True)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = cgmod.cg(b, tol=tol, max_iters=500, graph=True)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    ref = cgmod.cg(b[:oracle_batch].double(), tol=1e-9, max_iters=3000)
+    err = ((res.x[:oracle_batch].double() - ref.x).reshape(oracle_batch, -1).norm(dim=1)
+           / ref.x.reshape(oracle_batch, -1).norm(dim=1))
+    return {
+        "workload": f"plain CG, {batch} noisy {n}x{n} ellipse phantoms, tol {tol:g} on the normal equations",
+        "plain_solves_s": batch / el,
+        "plain_iters_mean": float(res.iterations.float().mean()),
+        "normal_residual_max": float(res.normal_residual.max()),
+        "data_residual_mean": float(res.data_residual.mean()),
+        "err_vs_float64_cg_mean": float(err.mean()),
+        "learned_solves_s": None,
+    }
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -327,6 +361,9 @@ def main():
         extras["adrt_f64_img_s"] = 64 * ks / t64
         extras["adrt_f64_gbs"] = 64 * ks * bytes_per_image(n, 8) / t64 / 1e9
         del y64, x64
+
+    if not args.no_extras and rank == 0:
+        extras["cg"] = cg_bench(torch, dev)
 
     peak, peak_src = load_peaks()
     bpi = bytes_per_image(n, 4)

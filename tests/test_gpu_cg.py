@@ -73,3 +73,14 @@ def test_warm_start_converges_faster():
     cold = cgmod.cg(b, tol=1e-5, max_iters=500)
     warm = cgmod.cg(b, x0=xt + 1e-3 * torch.randn_like(xt), tol=1e-5, max_iters=500)
     assert warm.iterations.sum() < cold.iterations.sum()
+
+
+def test_graphed_forward_matches_eager():
+    from adrt_gb300.graphs import GraphedCall
+
+    x = torch.rand((2, 1024, 1024), device="cuda")
+    g = GraphedCall(adrt.adrt, x.clone())
+    for seed in range(3):
+        torch.manual_seed(seed)
+        xn = torch.rand((2, 1024, 1024), device="cuda")
+        assert torch.equal(g(xn), adrt.adrt(xn))
