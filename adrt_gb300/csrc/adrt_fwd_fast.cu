@@ -552,6 +552,8 @@ unsigned *fast_error_word() {
 
 int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                       cudaStream_t st) {
+  const i64 per = (i64)fast_inter_bytes(n);
+  if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
   unsigned *err = fast_error_word();
   if (!err) return ADRT_GB300_ERR_CUDA;
   static bool configured = false;
@@ -560,9 +562,7 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
     cudaFuncSetAttribute(fast::pass_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
     configured = true;
   }
-  const i64 per = (i64)fast_inter_bytes(n);
   i64 chunk = fast_chunk(batch, n);
-  if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
   if ((i64)ws_bytes < per * chunk) chunk = (i64)ws_bytes / per;
   float *inter = static_cast<float *>(ws);
   const int cs = fast_cs(n);
