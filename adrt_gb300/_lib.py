@@ -72,6 +72,22 @@ SIGNATURES = {
     "adrt_gb300_batched_dot": [_v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
+    # learned preconditioner kernels (include/adrt_gb300_net.h)
+    "adrtnet_conv3x3": [_v, _int, _v, _int, _v, _v, _v, _int, _v, _i64, _i64, _i64, _v],
+    "adrtnet_conv3x3_wgrad": [_v, _int, _v, _int, _v, _i64, _i64, _i64, _v],
+    "adrtnet_status": [_v],
+    "adrtnet_conv_in": [_v, _v, _v, _v, _i64, _i64, _i64, _v],
+    "adrtnet_conv_in_wgrad": [_v, _v, _v, _v, _i64, _i64, _i64, _v],
+    "adrtnet_conv_out": [_v, _v, _v, _v, _i64, _i64, _i64, _v],
+    "adrtnet_conv_out_bwd": [_v, _v, _v, _v, _v, _v, _i64, _i64, _i64, _v],
+    "adrtnet_pool2": [_v, _v, _i64, _i64, _i64, _int, _v],
+    "adrtnet_pool2_bwd": [_v, _v, _v, _v, _i64, _i64, _i64, _int, _v],
+    "adrtnet_up2": [_v, _v, _i64, _i64, _i64, _int, _v],
+    "adrtnet_up2_bwd": [_v, _v, _v, _i64, _i64, _i64, _int, _v],
+    "adrtnet_bias_grad": [_v, _v, _i64, _int, _v],
+    "adrtnet_mse": [_v, _v, ctypes.c_float, _v, _v, _i64, _v],
+    "adrtnet_adam": [_v, _v, _v, _v, _v, _int, _i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, _v, _int, _v, _v],
 }
 _RESTYPES = {
     "adrt_gb300_status_string": ctypes.c_char_p,

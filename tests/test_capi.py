@@ -16,7 +16,7 @@ def _declared():
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
-        names |= set(re.findall(r"\b(adrt_gb300_\w+)\s*\(", text))
+        names |= set(re.findall(r"\b((?:adrt_gb300|adrtnet)_\w+)\s*\(", text))
     return sorted(names)
 
 
