@@ -72,6 +72,10 @@ SIGNATURES = {
     "adrt_gb300_batched_dot": [_v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
+    "adrt_gb300_tune_set": [_int, _int, _i64, _int, _int, _int, _int],
+    "adrt_gb300_tune_get": [_int, _int, _i64, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int),
+                            ctypes.POINTER(_int)],
+    "adrt_gb300_tune_reset": [],
     # learned preconditioner kernels (include/adrt_gb300_net.h)
     "adrtnet_conv3x3": [_v, _int, _v, _int, _v, _v, _v, _int, _v, _i64, _i64, _i64, _v],
     "adrtnet_conv3x3_wgrad": [_v, _int, _v, _int, _v, _i64, _i64, _i64, _v],
@@ -85,11 +89,13 @@ SIGNATURES = {
     "adrtnet_up2": [_v, _v, _i64, _i64, _i64, _int, _v],
     "adrtnet_up2_bwd": [_v, _v, _v, _i64, _i64, _i64, _int, _v],
     "adrtnet_bias_grad": [_v, _v, _i64, _int, _v],
-    "adrtnet_mse": [_v, _v, ctypes.c_float, _v, _v, _i64, _v],
+    "adrtnet_diff": [_v, _v, ctypes.c_float, _v, _i64, _v],
+    "adrtnet_loss_grad": [_v, _v, ctypes.c_float, ctypes.c_float, ctypes.c_float, _v, _v, _i64, _v],
     "adrtnet_adam": [_v, _v, _v, _v, _v, _int, _i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                      ctypes.c_float, _v, _int, _v, _v],
 }
 _RESTYPES = {
+    "adrt_gb300_tune_reset": None,
     "adrt_gb300_status_string": ctypes.c_char_p,
     "adrt_gb300_sumsq_workspace_size": _sz,
     "adrt_gb300_launch_count": ctypes.c_uint64,

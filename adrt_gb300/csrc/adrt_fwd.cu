@@ -25,14 +25,20 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tune.cuh"
 
 namespace adrtg {
 
 // Output offsets per tile: 256 for n >= 128, else 128 (narrow images waste
 // wide tiles; measured 2x faster at n = 32 with 128, 1.2-1.3x slower at
-// n = 128..256).
+// n = 128..256), unless the autotuner's table says otherwise.
 constexpr int kFwdWNarrow = 128, kFwdWWide = 256;
-static __host__ __device__ constexpr int fwd_width(long long n) { return n >= 128 ? kFwdWWide : kFwdWNarrow; }
+static int fwd_width(long long n, int dtype) {
+  const int w = tune_lookup(ADRT_GB300_OP_ADRT, dtype, n).width;
+  if (w == kFwdWNarrow || w == kFwdWWide) return w;
+  return n >= 128 ? kFwdWWide : kFwdWNarrow;
+}
+template <typename T> constexpr int dtype_code() { return sizeof(T) == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64; }
 constexpr int kFwdHalo = 32;  // halo columns kept left of the tile (>= 2^S - 1)
 constexpr int kFwdThreads = 256;
 
@@ -182,13 +188,9 @@ static __host__ __device__ i64 fwd_pass_tiles(i64 n, int S, int W) {
 
 // ---- host side --------------------------------------------------------------
 
-// Split L stages into passes of at most 5 stages, as even as possible.
-static int plan_passes(int L, int *sizes) {
-  if (L == 0) { sizes[0] = 0; return 1; }
-  const int P = (L + 4) / 5;
-  for (int p = 0; p < P; ++p) sizes[p] = L / P + (p < L % P ? 1 : 0);
-  return P;
-}
+// Split L stages into passes of at most 5 stages (or the tuned maximum), as
+// even as possible.
+static int plan_passes(int L, int *sizes, int max_fused = 5) { return plan_stage_split(L, max_fused, sizes); }
 
 template <typename T, int S, bool FIRST, bool LAST, int W>
 static int launch_fwd_pass_w(const FwdPassArgs &a, cudaStream_t st) {
@@ -207,7 +209,7 @@ static int launch_fwd_pass_w(const FwdPassArgs &a, cudaStream_t st) {
 
 template <typename T, int S, bool FIRST, bool LAST>
 static int launch_fwd_pass(const FwdPassArgs &a, cudaStream_t st) {
-  if (fwd_width(a.n) == kFwdWWide) return launch_fwd_pass_w<T, S, FIRST, LAST, kFwdWWide>(a, st);
+  if (fwd_width(a.n, dtype_code<T>()) == kFwdWWide) return launch_fwd_pass_w<T, S, FIRST, LAST, kFwdWWide>(a, st);
   return launch_fwd_pass_w<T, S, FIRST, LAST, kFwdWNarrow>(a, st);
 }
 
@@ -232,10 +234,12 @@ static int dispatch_pass(int S, bool first, bool last, const FwdPassArgs &a, cud
   return dispatch_S<T, false, false>(S, a, st);
 }
 
-// Images per chunk: the intermediate of one chunk is meant to stay in L2.
+// Images per chunk: the intermediate of one chunk is meant to stay in L2
+// (48 MB, or the tuned budget).
 static i64 fwd_chunk(i64 batch, i64 n, size_t elem) {
   const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
-  const size_t budget = (size_t)48 << 20;
+  const int mb = tune_lookup(ADRT_GB300_OP_ADRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).chunk_mb;
+  const size_t budget = (size_t)(mb > 0 ? mb : 48) << 20;
   i64 k = (i64)(budget / per);
   if (k < 1) k = 1;
   return k < batch ? k : batch;
@@ -253,10 +257,18 @@ int fwd_first_pass_padded(const float *in, float *inter, i64 batch, i64 n, int s
   return dispatch_pass<float>(stages, true, false, a, st);
 }
 
+static bool use_fast_path(i64 n, size_t elem) {
+  return fast_forward_eligible(n, elem) && tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).use_fast != 0;
+}
+
+static int fwd_max_fused(i64 n, size_t elem) {
+  return tune_lookup(ADRT_GB300_OP_ADRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).max_fused;
+}
+
 size_t fwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
-  if (fast_forward_eligible(n, elem)) return fast_workspace_bytes(batch, n);
+  if (use_fast_path(n, elem)) return fast_workspace_bytes(batch, n);
   int sizes[16];
-  const int P = plan_passes(num_iters(n), sizes);
+  const int P = plan_passes(num_iters(n), sizes, fwd_max_fused(n, elem));
   if (P <= 1) return 0;
   const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
   return per * (P >= 3 ? 2 : 1) * (size_t)fwd_chunk(batch, n, elem);
@@ -266,12 +278,12 @@ template <typename T>
 int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st) {
   if constexpr (sizeof(T) == 4) {
-    if (fast_forward_eligible(n, sizeof(T)))
+    if (use_fast_path(n, sizeof(T)))
       return adrt_forward_fast(reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out),
                                batch, n, ws, ws_bytes, st);
   }
   int sizes[16];
-  const int P = plan_passes(num_iters(n), sizes);
+  const int P = plan_passes(num_iters(n), sizes, fwd_max_fused(n, sizeof(T)));
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
   const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
   i64 chunk = fwd_chunk(batch, n, sizeof(T));

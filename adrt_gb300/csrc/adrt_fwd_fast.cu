@@ -24,6 +24,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tune.cuh"
 
 namespace adrtg {
 namespace fast {
@@ -517,11 +518,13 @@ size_t fast_inter_bytes(i64 n) { return sizeof(float) * 4 * (size_t)n * fast_cs(
 
 bool fast_forward_eligible(i64 n, size_t elem) { return elem == 4 && n >= 64 && n <= fast::N; }
 
-// Images per chunk so that the chunk's intermediate stays in L2 (~48 MB).
+// Images per chunk so that the chunk's intermediate stays in L2 (~48 MB;
+// 2 images at n = 1024), or the tuned budget.
 static i64 fast_chunk(i64 batch, i64 n) {
-  i64 k = (i64)((size_t)(48u << 20) / fast_inter_bytes(n));
+  const int mb = tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).chunk_mb;
+  i64 k = (i64)(((size_t)(mb > 0 ? mb : 48) << 20) / fast_inter_bytes(n));
   if (k < 1) k = 1;
-  if (n == fast::N) k = 2;
+  if (n == fast::N && mb == 0) k = 2;
   return batch < k ? batch : k;
 }
 

@@ -19,6 +19,7 @@
 // angle; stores go to a per-member shifted window.  Copy and zero rules are
 // evaluated on reference offsets, exactly as in the reference.
 #include "common.cuh"
+#include "tune.cuh"
 
 namespace adrtg {
 
@@ -154,11 +155,10 @@ bwd_pass_kernel(BwdPassArgs args) {
   }
 }
 
-static int plan_passes_bwd(int L, int *sizes) {
-  if (L == 0) { sizes[0] = 0; return 1; }
-  const int P = (L + 4) / 5;
-  for (int p = 0; p < P; ++p) sizes[p] = L / P + (p < L % P ? 1 : 0);
-  return P;
+// Passes of at most 5 stages (or the tuned maximum), as even as possible.
+static int plan_passes_bwd(i64 n, size_t elem, int *sizes) {
+  const int mf = tune_lookup(ADRT_GB300_OP_BDRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).max_fused;
+  return plan_stage_split(num_iters(n), mf, sizes);
 }
 
 template <typename T, int S, bool FIRST, bool LAST>
@@ -203,7 +203,8 @@ static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cuda
 
 static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
   const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
-  const size_t budget = (size_t)48 << 20;
+  const int mb = tune_lookup(ADRT_GB300_OP_BDRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).chunk_mb;
+  const size_t budget = (size_t)(mb > 0 ? mb : 48) << 20;
   i64 k = (i64)(budget / per);
   if (k < 1) k = 1;
   return k < batch ? k : batch;
@@ -211,7 +212,7 @@ static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
 
 size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
   int sizes[16];
-  const int P = plan_passes_bwd(num_iters(n), sizes);
+  const int P = plan_passes_bwd(n, elem, sizes);
   if (P <= 1) return 0;
   const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
   return per * (P >= 3 ? 2 : 1) * (size_t)bwd_chunk(batch, n, elem);
@@ -221,7 +222,7 @@ template <typename T>
 int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st) {
   int sizes[16];
-  const int P = plan_passes_bwd(num_iters(n), sizes);
+  const int P = plan_passes_bwd(n, sizeof(T), sizes);
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
   const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
   i64 chunk = bwd_chunk(batch, n, sizeof(T));

@@ -301,15 +301,24 @@ __global__ void bias_grad_kernel(const bf16 *g, float *db, int c, long long npix
   }
 }
 
-// Loss = mean((scale * out - target)^2); g = d loss / d out.
-__global__ void mse_kernel(const float *out, const float *target, float scale, float *g, float *loss,
-                           long long n) {
+// d = scale * out - target.
+__global__ void diff_kernel(const float *out, const float *target, float scale, float *d, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = scale * out[i] - target[i];
+}
+
+// Loss (alpha * d.d + mu * d.e) / n added to *loss, and its gradient with
+// respect to out, g = 2 * scale * (alpha * d + mu * e) / n, where e is a
+// symmetric positive semi-definite operator applied to d (e may be null).
+__global__ void loss_grad_kernel(const float *d, const float *e, float alpha, float mu, float scale, float *g,
+                                 float *loss, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   float l = 0.0f;
   if (i < n) {
-    const float d = scale * out[i] - target[i];
-    g[i] = 2.0f * d * scale / (float)n;
-    l = d * d / (float)n;
+    const float di = d[i];
+    const float ei = e ? e[i] : 0.0f;
+    g[i] = 2.0f * scale * (alpha * di + mu * ei) / (float)n;
+    l = (alpha * di * di + mu * di * ei) / (float)n;
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
@@ -459,11 +468,18 @@ int adrtnet_bias_grad(const void *g, float *db, int64_t npix, int c, void *strea
   return launch_status();
 }
 
-int adrtnet_mse(const float *out, const float *target, float scale, float *g, float *loss, int64_t n,
-                void *stream) {
-  if (!out || !target || !g) return ADRT_GB300_ERR_NULL;
+int adrtnet_diff(const float *out, const float *target, float scale, float *d, int64_t n, void *stream) {
+  if (!out || !target || !d) return ADRT_GB300_ERR_NULL;
   if (n < 1) return ADRT_GB300_ERR_SHAPE;
-  mse_kernel<<<blocks(n, 256), 256, 0, S(stream)>>>(out, target, scale, g, loss, n);
+  diff_kernel<<<blocks(n, 256), 256, 0, S(stream)>>>(out, target, scale, d, n);
+  return launch_status();
+}
+
+int adrtnet_loss_grad(const float *d, const float *e, float alpha, float mu, float scale, float *g, float *loss,
+                      int64_t n, void *stream) {
+  if (!d || !g) return ADRT_GB300_ERR_NULL;
+  if (n < 1) return ADRT_GB300_ERR_SHAPE;
+  loss_grad_kernel<<<blocks(n, 256), 256, 0, S(stream)>>>(d, e, alpha, mu, scale, g, loss, n);
   return launch_status();
 }
 

@@ -37,7 +37,7 @@ from . import _lib
 from ._ops import adrt as _adrt
 from .autograd import _adjoint_raw as _adjoint
 
-__all__ = ["PreconditionerNet", "LAYERS", "training_pairs", "learned_cg", "TrainLog"]
+__all__ = ["PreconditionerNet", "LAYERS", "training_pairs", "train", "learned_cg", "normal_op_norm", "TrainLog"]
 
 # Tensor-core layers: name -> (c_in, c_out).  Level l works at (h >> l, w >> l).
 LAYERS = (
@@ -143,6 +143,7 @@ class PreconditionerNet:
         self.step_count = torch.zeros(1, dtype=torch.int64, device=self.dev)
         self.wbuf = torch.empty(max(1, woff), dtype=torch.bfloat16, device=self.dev)
         self.in_scale = 1.0
+        self.loss_terms = (1.0, 0.0, 0)  # (alpha, mu, k): see loss_and_grad
         self._bufs = {}
         self.refresh_weights()
 
@@ -193,6 +194,7 @@ class PreconditionerNet:
             b[nm] = act(lv, c)
         b["out"] = torch.empty((B, H, W), dtype=torch.float32, device=self.dev)
         b["gout"] = torch.empty((B, H, W), dtype=torch.float32, device=self.dev)
+        b["dres"] = torch.empty((B, H, W), dtype=torch.float32, device=self.dev)
         b["loss"] = torch.zeros(1, dtype=torch.float32, device=self.dev)
         self._bufs[key] = b
         return b
@@ -318,11 +320,24 @@ class PreconditionerNet:
         _lib.check(rc, "adrtnet_adam")
 
     def loss_and_grad(self, out, target, scale=1.0):
+        """Loss and d loss / d out for d = scale * out - target:
+        (alpha |d|^2 + mu d.(A^T A)^k d) / numel, with (alpha, mu, k) =
+        self.loss_terms.  k = 0 is the mean squared error; k = 1 adds the
+        energy norm |A d|^2 that CG on the normal equations minimises; k = 2
+        the normal-equation residual |A^T A d|^2 that its stopping rule
+        measures."""
         b = self._buffers(*out.shape)
         b["loss"].zero_()
-        rc = self.lib.adrtnet_mse(_p(out), _p(target), scale, _p(b["gout"]), _p(b["loss"]), out.numel(),
-                                  _stream(self.dev))
-        _lib.check(rc, "adrtnet_mse")
+        n = out.numel()
+        self._call("adrtnet_diff", _p(out), _p(target), scale, _p(b["dres"]), n)
+        alpha, mu, k = self.loss_terms
+        e = None
+        if k > 0 and mu != 0.0:
+            e = b["dres"]
+            for _ in range(k):
+                e = _adjoint(_adrt(e))
+        self._call("adrtnet_loss_grad", _p(b["dres"]), _p(e), alpha, mu if e is not None else 0.0, scale,
+                   _p(b["gout"]), _p(b["loss"]), n)
         return b["gout"], b["loss"]
 
     def train_step(self, u, target, lr=1e-3):
@@ -406,18 +421,39 @@ def training_pairs(count: int, n: int, seed: int, noise: float = 1e-3, tol: floa
     return torch.cat(bs), torch.cat(xs)
 
 
+def normal_op_norm(n: int, device="cuda", iters: int = 30) -> float:
+    """Largest eigenvalue of A^T A on n x n images (power iteration)."""
+    g = torch.Generator(device=device)
+    g.manual_seed(12345)
+    x = torch.rand((1, n, n), generator=g, device=device)
+    lam = 0.0
+    for _ in range(iters):
+        y = _adjoint(_adrt(x))
+        lam = float(y.norm() / x.norm())
+        x = y / y.norm()
+    return lam
+
+
 def train(net: PreconditionerNet, b: torch.Tensor, x_cg: torch.Tensor, *, epochs: int = 10, batch: int = 16,
-          lr: float = 1e-3, seed: int = 0, graph: bool = True) -> TrainLog:
+          lr: float = 1e-3, seed: int = 0, graph: bool = True, loss_power: int = 0, loss_mu: float = 1.0,
+          loss_alpha: float = 1.0) -> TrainLog:
     """Fits u = s * A^T b -> x_cg; s is set from the data so that u and x_cg
-    have the same mean norm.  Learning rate `lr` for the first 70 % of the
-    epochs, lr / 10 after (each phase one captured training step)."""
+    have the same mean norm.  Loss: loss_alpha |d|^2 + loss_mu d.(A^T A /
+    lambda_max)^loss_power d for d = x0 - x_cg.  Learning rate `lr` for the
+    first 70 % of the epochs, lr / 10 after (each phase one captured
+    training step)."""
     import time
 
+    n = b.shape[-1]
+    if loss_power > 0:
+        lam = normal_op_norm(n, net.dev)
+        net.loss_terms = (loss_alpha, loss_mu / lam ** loss_power, loss_power)
+    else:
+        net.loss_terms = (loss_alpha, 0.0, 0)
     bt = _adjoint(b.contiguous())
     net.in_scale = float(x_cg.norm() / bt.norm())
     u_all = bt * net.in_scale
     N = u_all.shape[0]
-    n = u_all.shape[-1]
     gen = torch.Generator(device="cpu").manual_seed(seed)
     losses = []
     steps = 0

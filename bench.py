@@ -161,38 +161,69 @@ def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
     }
 
 
-def cg_bench(torch, dev, n=256, batch=512, oracle_batch=32, tol=1e-4):
-    """Plain batched CG on the normal equations for noisy 256 x 256 phantoms:
-    solves/s to ||A^T(Ax-b)|| / ||A^T b|| <= tol, plus the data residual and
-    the error against a float64 CG solution of the same systems."""
+def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=30):
+    """Plain and learned-start batched CG on the normal equations of noisy
+    256 x 256 ellipse phantoms (data b = adrt(x) + N(0, (1e-3 max|b|)^2)).
+
+    Solves/s = test images / wall time to ||A^T(Ax-b)|| / ||A^T b|| <= tol
+    for every image (the learned arm includes the network's forward pass).
+    The network is trained here first on pairs the method generates
+    (phantom -> adrt -> noise -> plain CG to 1e-5), untimed."""
     import adrt_gb300 as adrt
     from adrt_gb300 import cg as cgmod
-    from adrt_gb300.data import ellipse_phantoms
+    from adrt_gb300 import learned
 
-    xt = ellipse_phantoms(batch, n, seed=900_000, device=dev)
-    b = adrt.adrt(xt)
-    sigma = 1e-3 * b.abs().amax(dim=(1, 2, 3), keepdim=True)
-    g = torch.Generator(device=dev)
-    g.manual_seed(4242)
-    b = b + sigma * torch.randn(b.shape, generator=g, device=dev)
-    cgmod.cg(b[:8], tol=tol, max_iters=200, graph=True)  # warm
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = cgmod.cg(b, tol=tol, max_iters=500, graph=True)
-    torch.cuda.synchronize()
-    el = time.perf_counter() - t0
-    ref = cgmod.cg(b[:oracle_batch].double(), tol=1e-9, max_iters=3000)
-    err = ((res.x[:oracle_batch].double() - ref.x).reshape(oracle_batch, -1).norm(dim=1)
-           / ref.x.reshape(oracle_batch, -1).norm(dim=1))
-    return {
-        "workload": f"plain CG, {batch} noisy {n}x{n} ellipse phantoms, tol {tol:g} on the normal equations",
-        "plain_solves_s": batch / el,
-        "plain_iters_mean": float(res.iterations.float().mean()),
-        "normal_residual_max": float(res.normal_residual.max()),
-        "data_residual_mean": float(res.data_residual.mean()),
-        "err_vs_float64_cg_mean": float(err.mean()),
-        "learned_solves_s": None,
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    b_te, _ = learned.training_pairs(n_test, n, seed=900_000, tol=1e-5, device=dev)
+    cgmod.cg(b_te[:16], tol=tol, max_iters=200, graph=True)  # warm
+    plain, t_plain = timed(lambda: cgmod.cg(b_te, tol=tol, max_iters=500, graph=True))
+    ref = cgmod.cg(b_te[:oracle_batch].double(), tol=1e-9, max_iters=3000)
+
+    def err(x):
+        d = x[:oracle_batch].double() - ref.x
+        return float((d.reshape(oracle_batch, -1).norm(dim=1) / ref.x.reshape(oracle_batch, -1).norm(dim=1)).mean())
+
+    def solved(r):
+        # A solve counts when the recomputed residual meets the tolerance
+        # (1 % slack for the float32 recomputation).
+        return int((r.normal_residual <= 1.01 * tol).sum())
+
+    out = {
+        "workload": f"{n_test} noisy {n}x{n} ellipse phantoms, tol {tol:g} on the normal equations",
+        "plain_solves_s": solved(plain) / t_plain,
+        "plain_solved": solved(plain),
+        "plain_iters_mean": float(plain.iterations.float().mean()),
+        "plain_normal_residual_max": float(plain.normal_residual.max()),
+        "plain_data_residual_mean": float(plain.data_residual.mean()),
+        "plain_err_vs_float64_cg": err(plain.x),
     }
+    t0 = time.perf_counter()
+    b_tr, x_tr = learned.training_pairs(n_train, n, seed=1, tol=1e-5, device=dev)
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t0
+    net = learned.PreconditionerNet(dev, seed=0)
+    log = learned.train(net, b_tr, x_tr, epochs=epochs, batch=16, lr=3e-4)
+    del b_tr, x_tr
+    learned.learned_cg(net, b_te[:16], tol=tol, max_iters=200)  # warm
+    lrn, t_lrn = timed(lambda: learned.learned_cg(net, b_te, tol=tol, max_iters=500))
+    out.update({
+        "learned_solves_s": solved(lrn) / t_lrn,
+        "learned_solved": solved(lrn),
+        "learned_iters_mean": float(lrn.iterations.float().mean()),
+        "learned_normal_residual_max": float(lrn.normal_residual.max()),
+        "learned_data_residual_mean": float(lrn.data_residual.mean()),
+        "learned_err_vs_float64_cg": err(lrn.x),
+        "learned_over_plain": (solved(lrn) / t_lrn) / (solved(plain) / t_plain),
+        "training": {"pairs": n_train, "pair_seconds": t_pairs, "epochs": epochs, "steps": log.steps,
+                     "seconds": log.seconds, "loss_first": log.losses[0], "loss_last": log.losses[-1]},
+    })
+    return out
 
 
 def run_reference(args):
@@ -246,6 +277,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch configuration)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -282,6 +314,15 @@ def main():
         return float(t.item())
 
     n, B = args.n, args.batch
+    tuned = None
+    if not args.no_tune:
+        from adrt_gb300 import tune
+
+        r = tune.autotune("adrt", n, torch.float32, batch=min(B, 32), reps=5, device=dev)
+        tuned = {"config": {"width": r.best.width, "max_fused": r.best.max_fused, "chunk_mb": r.best.chunk_mb,
+                            "use_fast": r.best.use_fast},
+                 "best_ms": r.best_ms, "default_ms": r.default_ms, "candidates": len(r.timings),
+                 "batch": min(B, 32)}
     x = mixed_batch(B, n, seed=1000 * rank, device=dev, dtype=torch.float32)
     torch.cuda.synchronize()
 
@@ -402,6 +443,7 @@ def main():
             "bytes_per_image": bpi,
         },
         "e2e": e2e,
+        "autotune": tuned,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }

@@ -65,6 +65,20 @@ int adrt_gb300_num_iters(int64_t n);
  * loaded (all threads, all devices).  For accounting; no reference counterpart. */
 uint64_t adrt_gb300_launch_count(void);
 
+/* Autotuner table (no reference counterpart; the reference has one CPU code
+ * path).  Per (op in {ADRT_GB300_OP_ADRT, ADRT_GB300_OP_BDRT}, dtype, n a
+ * power of two): width = forward tile width in offsets (0, 128 or 256),
+ * max_fused = stages fused in shared memory per pass (0 = built-in 5, or
+ * 1..5), chunk_mb = L2 budget of one chunk's intermediate in MB (0 =
+ * built-in), use_fast = float32 fast forward kernels (-1 = when eligible,
+ * 0 = off, 1 = on when eligible).  Results are bit-identical for every
+ * setting; only speed changes.  Not synchronised with calls in flight on
+ * other threads: set the table before launching work.  Workspace sizes
+ * depend on it, so query them after setting it. */
+int adrt_gb300_tune_set(int op, int dtype, int64_t n, int width, int max_fused, int chunk_mb, int use_fast);
+int adrt_gb300_tune_get(int op, int dtype, int64_t n, int *width, int *max_fused, int *chunk_mb, int *use_fast);
+void adrt_gb300_tune_reset(void);
+
 /* Synchronises `stream`, then reports ADRT_GB300_ERR_TIMEOUT (and clears the
  * condition) if a kernel of this library on the current device gave up a
  * bounded wait for its bulk copies since the last call; ADRT_GB300_OK

@@ -76,10 +76,13 @@ int adrtnet_up2_bwd(const void *g_high, const void *mask, void *out, int64_t bat
 /* db[c] += sum over npix pixels of g[p][c] (bf16 NHWC, c a multiple of 32). */
 int adrtnet_bias_grad(const void *g, float *db, int64_t npix, int c, void *stream);
 
-/* Training loss mean((scale * out - target)^2) added to *loss (may be NULL),
- * and g = its gradient with respect to out. */
-int adrtnet_mse(const float *out, const float *target, float scale, float *g, float *loss, int64_t n,
-                void *stream);
+/* Training loss, two steps: d = scale * out - target; then, with e = K d
+ * for a symmetric positive semi-definite K the caller applies (e may be
+ * NULL), loss += (alpha d.d + mu d.e) / n (loss may be NULL) and
+ * g = 2 scale (alpha d + mu e) / n, the gradient with respect to out. */
+int adrtnet_diff(const float *out, const float *target, float scale, float *d, int64_t n, void *stream);
+int adrtnet_loss_grad(const float *d, const float *e, float alpha, float mu, float scale, float *g, float *loss,
+                      int64_t n, void *stream);
 
 /* A run of the flat f32 parameter vector.  Conv segments hold weights
  * [9][c_out][c_in]; the Adam kernel also writes their bf16 copies at
