@@ -35,10 +35,15 @@ constexpr int TW = W + HALO;      // 512 tile positions
 constexpr int NCH = TW / 4;       // 128 chunks of 4 positions
 constexpr int RS = 4 * (NCH + 1); // exchange row stride in floats (odd chunk count)
 constexpr int NT = 256;           // threads per CTA
-constexpr int CS = 2048;          // row stride of the intermediate buffer (>= 2n-1, 32-byte multiple)
 constexpr int N = 1024;
 constexpr int C = 2 * N - 1;
-constexpr int COL_TILES = (C + W - 1) / W;  // 5
+constexpr int COL_TILES = (C + W - 1) / W;  // 5 output tiles of pass B
+// After five stages a row group's values are non-zero only at offsets below
+// n + 31 (shifts reach 31); beyond that every value is +0, the sum of the
+// zero padding.  Pass A computes the tiles that hold those offsets and the
+// intermediate rows end there: pass B reads anything past the row end as +0.
+constexpr int A_TILES = (N + 31 + W - 1) / W;  // 3
+constexpr int CS = A_TILES * W;                // 1440: intermediate row stride (32-byte multiple)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 
@@ -453,7 +458,7 @@ __global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__
                                                        float *__restrict__ inter, int nimg) {
   extern __shared__ __align__(16) float xs[];
   int t = blockIdx.x;
-  const int ct = t % COL_TILES; t /= COL_TILES;
+  const int ct = t % A_TILES; t /= A_TILES;
   const int r = t % 32; t /= 32;
   const int q = t % 4; t /= 4;
   const int bimg = t;
@@ -509,9 +514,10 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
 
 }  // namespace fast
 
-// Row stride of the fast path's intermediate: 2n-1 offsets rounded up to a
-// multiple of 8 floats (32 bytes) so every row start is 256-bit aligned.
-static int fast_cs(i64 n) { return (int)(((2 * n - 1) + 7) / 8 * 8); }
+// Row stride of the fast path's intermediate: at n = 1024 the offsets pass A
+// writes (fast::CS); below, 2n-1 offsets rounded up to a multiple of 8 floats
+// (32 bytes) so every row start is 256-bit aligned.
+static int fast_cs(i64 n) { return n == fast::N ? fast::CS : (int)(((2 * n - 1) + 7) / 8 * 8); }
 
 // Bytes of intermediate per image: [q][32][n/32][cs] float32.
 size_t fast_inter_bytes(i64 n) { return sizeof(float) * 4 * (size_t)n * fast_cs(n); }
@@ -575,7 +581,7 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
     const int nb = (int)((batch - b0) < chunk ? (batch - b0) : chunk);
     int rc;
     if (n == fast::N) {
-      const unsigned grid = (unsigned)(nb * 4 * 32 * fast::COL_TILES);
+      const unsigned grid = (unsigned)(nb * 4 * 32 * fast::A_TILES);
       fast::pass_a_kernel<<<grid, fast::NT, fast::SMEM, st>>>(in + b0 * n * n, inter, nb);
       rc = launch_status();
     } else {

@@ -83,7 +83,7 @@ def candidates(op: str, n: int, dtype) -> list:
     """Configurations worth timing for (op, n, dtype); the built-in one first."""
     L = max(0, n.bit_length() - 1)
     fused = [0] + [m for m in (4, 3) if m < L and -(-L // m) != -(-L // 5)]
-    chunks = [0, 24, 96]
+    chunks = [0, 24, 72, 96]
     out = [Config()]
     if op == "adrt":
         fast = [-1, 0] if (_dt(dtype) == _lib.F32 and 64 <= n <= 1024) else [-1]
