@@ -46,6 +46,7 @@ constexpr int A_TILES = (N + 31 + W - 1) / W;  // 3
 constexpr int CS = A_TILES * W;                // 1440: intermediate row stride (32-byte multiple)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
+static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange buffer");
 
 __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
 
@@ -432,25 +433,57 @@ __device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, i
   }
 }
 
+// Pass B output staging: the CTA's tile (W offsets x 32 angles, 128-byte
+// rows) goes through shared memory so that the (4, 2n-1, n) output is written
+// with whole 128-byte row segments.  Group-2 lanes own rows 8 apart (block b
+// = rows 8b..8b+7), so the 16-byte chunk index is XOR-swizzled with
+// (row >> 3) & 7: the eight lanes of a quarter-warp then hit eight different
+// bank groups when writing, and a row's eight chunks are distinct when read.
+__device__ __forceinline__ int ost_chunk(int row, int c) { return c ^ ((row >> 3) & 7); }
+
 template <int L1>
-__device__ __forceinline__ void group2_passB(const float *xs, float *dst_q, int ap, int c0, int n) {
+__device__ __forceinline__ void group2_passB(const float *xs, float *ost, int c0, int n) {
   int b;
   bool active, store;
   group2_lane(b, active, store);
   float out[8][8];
   group2_compute<L1, 0>(xs, b, active, out);
+  __syncthreads();  // every warp is done reading the exchange rows
   if (!store) return;
-  const int d0 = c0 + 8 * b;
+  // Rows 8b..8b+7 share the swizzle term b & 7: fixed offsets from one base.
+  const int sw = b & 7;
+  float *p0 = ost + 8 * b * 32 + 4 * ((2 * L1) ^ sw);
+  float *p1 = ost + 8 * b * 32 + 4 * ((2 * L1 + 1) ^ sw);
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const int d = d0 + k;
-    if (d < 2 * n - 1) {
-      float v[8];
-#pragma unroll
-      for (int l = 0; l < 8; ++l) v[l] = out[l][k];
-      st8_stream(dst_q + (size_t)d * n + ap * 32 + 8 * L1, v);
-    }
+    *reinterpret_cast<float4 *>(p0 + 32 * k) = make_float4(out[0][k], out[1][k], out[2][k], out[3][k]);
+    *reinterpret_cast<float4 *>(p1 + 32 * k) = make_float4(out[4][k], out[5][k], out[6][k], out[7][k]);
   }
+  (void)c0;
+  (void)n;
+}
+
+// Writes the staged tile: quarter-warps store one 128-byte row each.  Thread
+// t handles chunk t & 7 of rows (t >> 3) + 32 i, i < W / 32; the row's swizzle
+// term ((row >> 3) & 7) then only alternates between two values.  All shared
+// loads are issued before the global stores.
+__device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q, int ap, int c0, int n) {
+  constexpr int IT = W / 32;  // 15
+  static_assert(W % 32 == 0, "tile rows must split into 32-row steps");
+  const int r0 = threadIdx.x >> 3, c = threadIdx.x & 7;
+  const int sw0 = ((r0 >> 3) & 7), sw1 = (((r0 + 32) >> 3) & 7);
+  const float *s0 = ost + r0 * 32 + 4 * (c ^ sw0);
+  const float *s1 = ost + (r0 + 32) * 32 + 4 * (c ^ sw1);
+  float4 v[IT];
+#pragma unroll
+  for (int i = 0; i < IT; ++i)
+    v[i] = *reinterpret_cast<const float4 *>((i & 1 ? s1 : s0) + (i >> 1) * 64 * 32);
+  const int rows = min(W, 2 * n - 1 - c0);
+  float *d = dst_q + (size_t)(c0 + r0) * n + ap * 32 + 4 * c;
+  const size_t step = (size_t)32 * n;
+#pragma unroll
+  for (int i = 0; i < IT; ++i)
+    if (r0 + 32 * i < rows) __stcs(reinterpret_cast<float4 *>(d + i * step), v[i]);
 }
 
 // inter layout: [image][q][row group g (32)][angle a (32)][CS]
@@ -504,12 +537,16 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
   }
   __syncthreads();
   float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
+  // The output tile is staged over the exchange rows once all warps have
+  // read them (barrier inside group2_passB).
   switch ((threadIdx.x >> 5) & 3) {
-    case 0: group2_passB<0>(xs, dst_q, ap, c0, n); break;
-    case 1: group2_passB<1>(xs, dst_q, ap, c0, n); break;
-    case 2: group2_passB<2>(xs, dst_q, ap, c0, n); break;
-    default: group2_passB<3>(xs, dst_q, ap, c0, n); break;
+    case 0: group2_passB<0>(xs, xs, c0, n); break;
+    case 1: group2_passB<1>(xs, xs, c0, n); break;
+    case 2: group2_passB<2>(xs, xs, c0, n); break;
+    default: group2_passB<3>(xs, xs, c0, n); break;
   }
+  __syncthreads();
+  passB_store_tile(xs, dst_q, ap, c0, n);
 }
 
 }  // namespace fast
