@@ -33,6 +33,7 @@ struct BwdPassArgs {
   i64 n;
   int k0;          // first forward stage covered by this pass
   i64 batch;
+  i64 c_need;      // pass outputs are needed at reference offsets < c_need
 };
 
 // Buffer layout between passes, per (b, q): [angle s][section p][offset c],
@@ -77,8 +78,9 @@ bwd_pass_kernel(BwdPassArgs args) {
   const int q = (int)(t % 4); t /= 4;
   const i64 b = t;
   const i64 c0 = (i64)ct * kBwdW;
-  // Skip tiles that hold no member's valid offsets.
-  if (c0 >= C + ap * (ROWS - 1)) return;
+  // Skip tiles that hold no member's needed offsets (member i of this tile
+  // stores reference offsets >= c0 - a'*i).
+  if (c0 >= args.c_need + ap * (ROWS - 1)) return;
 
   // ---- load angle l = a'*2^S + l of section r, tile positions [c0, c0+TWP).
   if (FIRST) {
@@ -218,9 +220,14 @@ size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
   return per * (P >= 3 ? 2 : 1) * (size_t)bwd_chunk(batch, n, elem);
 }
 
+// rows_needed: offsets of each quadrant of the result the caller reads (2n-1
+// for bdrt itself, n for the adjoint, which truncates).  Undoing forward stage
+// k reads offsets at most 2^k to the right of the one it writes, so the pass
+// starting at forward stage k0 only has to produce offsets below
+// rows_needed + 2^k0 - 1; tiles beyond are skipped and left unwritten.
 template <typename T>
 int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
-                 cudaStream_t st) {
+                 cudaStream_t st, i64 rows_needed) {
   int sizes[16];
   const int P = plan_passes_bwd(n, sizeof(T), sizes);
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
@@ -244,7 +251,9 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
       const int p = P - 1 - s;
       const bool first = s == 0, last = s == P - 1;
       void *dst = last ? static_cast<void *>(out + b0 * 4 * n * (2 * n - 1)) : bufs[s & 1];
-      BwdPassArgs a{src, dst, n, kstart[p], nb};
+      const i64 C = 2 * n - 1;
+      const i64 need = rows_needed + (i64(1) << kstart[p]) - 1;
+      BwdPassArgs a{src, dst, n, kstart[p], nb, need < C ? need : C};
       int rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
       if (rc) return rc;
       src = dst;
@@ -253,7 +262,7 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   return ADRT_GB300_OK;
 }
 
-template int bdrt_forward<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t);
-template int bdrt_forward<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t);
+template int bdrt_forward<float>(const float *, float *, i64, i64, void *, size_t, cudaStream_t, i64);
+template int bdrt_forward<double>(const double *, double *, i64, i64, void *, size_t, cudaStream_t, i64);
 
 }  // namespace adrtg

@@ -5,7 +5,7 @@
 
 namespace adrtg {
 template <typename T> int adrt_forward(const T *, T *, i64, i64, void *, size_t, cudaStream_t);
-template <typename T> int bdrt_forward(const T *, T *, i64, i64, void *, size_t, cudaStream_t);
+template <typename T> int bdrt_forward(const T *, T *, i64, i64, void *, size_t, cudaStream_t, i64 rows_needed);
 template <typename T> int adrt_step_launch(const T *, T *, i64, i64, int, cudaStream_t);
 template <typename T> int bdrt_step_launch(const T *, T *, i64, i64, int, cudaStream_t);
 template <typename T> int iadrt_launch(const T *, T *, i64, i64, void *, size_t, cudaStream_t);
@@ -136,8 +136,8 @@ int adrt_gb300_bdrt(const void *in, void *out, int64_t batch, int64_t n, int dty
   if (!in || !out) return ADRT_GB300_ERR_NULL;
   if ((rc = check_dtype(dtype)) || (rc = check_adrt_shape(batch, n))) return rc;
   return DISPATCH(dtype,
-                  bdrt_forward<float>((const float *)in, (float *)out, batch, n, ws, ws_bytes, S(stream)),
-                  bdrt_forward<double>((const double *)in, (double *)out, batch, n, ws, ws_bytes, S(stream)));
+                  bdrt_forward<float>((const float *)in, (float *)out, batch, n, ws, ws_bytes, S(stream), 2 * n - 1),
+                  bdrt_forward<double>((const double *)in, (double *)out, batch, n, ws, ws_bytes, S(stream), 2 * n - 1));
 }
 
 int adrt_gb300_bdrt_step(const void *in, void *out, int64_t batch, int64_t n, int step,
@@ -173,11 +173,12 @@ int adrt_gb300_adjoint(const void *in, void *out, int64_t batch, int64_t n, int 
   void *bws = static_cast<char *>(ws) + ybytes;
   const size_t bws_bytes = ws_bytes - ybytes;
   if (dtype == ADRT_GB300_F32) {
-    if ((rc = bdrt_forward<float>((const float *)in, (float *)y, batch, n, bws, bws_bytes, S(stream))))
+    // Only the top n offsets of each quadrant reach the quadrant sum.
+    if ((rc = bdrt_forward<float>((const float *)in, (float *)y, batch, n, bws, bws_bytes, S(stream), n)))
       return rc;
     return quad_sum_launch<float>((const float *)y, (float *)out, batch, n, S(stream));
   }
-  if ((rc = bdrt_forward<double>((const double *)in, (double *)y, batch, n, bws, bws_bytes, S(stream))))
+  if ((rc = bdrt_forward<double>((const double *)in, (double *)y, batch, n, bws, bws_bytes, S(stream), n)))
     return rc;
   return quad_sum_launch<double>((const double *)y, (double *)out, batch, n, S(stream));
 }

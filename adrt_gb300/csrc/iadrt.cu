@@ -17,45 +17,95 @@
 
 namespace adrtg {
 
+// Loads for a chain never depend on its running value, so each thread keeps
+// the operands of the next U rows in a register ring (slot u holds row
+// row0 - u): the latency of a load is hidden behind U serial steps instead of
+// stalling every step.  Threads are ordered so that the first n/2 of a plane
+// run even-l chains and the rest odd-l chains: warps do not diverge between
+// the two recurrences.
+template <typename T> struct IadrtRing { static constexpr int U = sizeof(T) == 4 ? 16 : 8; };
+
+template <typename T>
+__device__ __forceinline__ T ld_or_zero(const T *p, bool ok) { return ok ? __ldg(p) : T(0); }
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i64 n, int s) {
+  constexpr int U = IadrtRing<T>::U;
   const i64 R = 2 * n - 1;
   const i64 Cc = n >> s;           // input chains per l
   const i64 C2 = Cc >> 1;          // output chains per l
-  const i64 chains = n;            // per plane, at every stage
+  const i64 half = n >> 1;         // even-l (and odd-l) chains per plane
   const i64 gid = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  if (gid >= planes * chains) return;
-  const i64 plane = gid / chains;
-  const i64 ch = gid % chains;
-  const i64 l = ch / C2, col = ch % C2;
+  if (gid >= planes * n) return;
+  const i64 plane = gid / n;
+  const i64 t = gid % n;
+  const bool odd = t >= half;
+  const i64 tt = odd ? t - half : t;
+  const i64 l = 2 * (tt / C2) + (odd ? 1 : 0), col = tt % C2;
+  const i64 ch = l * C2 + col;
   const i64 pl = l >> 1;
   const T *src = in + plane * R * n;
   T *dst = out + plane * R * n;
   const i64 e_ch = pl * Cc + 2 * col;
   const i64 o_ch = e_ch + 1;
+  T ea[U], oa[U];
   T prev = T(0);
-  if ((l & 1) == 0) {
-    for (i64 row = R - 1; row >= 0; --row) {
-      T v = add_rn(T(0), src[row * n + e_ch]);
-      if (row + 1 < R) {
-        v = sub_rn(v, src[(row + 1) * n + o_ch]);
-        v = add_rn(v, prev);
+  if (!odd) {
+    // v = (0 + E[row]) - O[row + 1] + prev   (O and prev only if row + 1 < R)
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const i64 r = R - 1 - u;
+      ea[u] = ld_or_zero(src + r * n + e_ch, r >= 0);
+      oa[u] = ld_or_zero(src + (r + 1) * n + o_ch, r >= 0 && r + 1 < R);
+    }
+    for (i64 row0 = R - 1; row0 >= 0; row0 -= U) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const i64 row = row0 - u;
+        if (row >= 0) {
+          T v = add_rn(T(0), ea[u]);
+          if (row + 1 < R) {
+            v = sub_rn(v, oa[u]);
+            v = add_rn(v, prev);
+          }
+          dst[row * n + ch] = v;
+          prev = v;
+        }
+        const i64 r = row - U;
+        ea[u] = ld_or_zero(src + r * n + e_ch, r >= 0);
+        oa[u] = ld_or_zero(src + (r + 1) * n + o_ch, r >= 0);
       }
-      dst[row * n + ch] = v;
-      prev = v;
     }
   } else {
+    // v = (0 + O[row + d]) - E[row + d]  (if row + d < R, else 0); v += prev (row + 1 < R)
     const i64 d = 1 + col;
-    for (i64 row = R - 1; row >= 0; --row) {
-      T v = T(0);
-      if (row + d < R) {
-        v = add_rn(v, src[(row + d) * n + o_ch]);
-        v = sub_rn(v, src[(row + d) * n + e_ch]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const i64 r = R - 1 - u + d;
+      const bool ok = r < R && r >= d;
+      ea[u] = ld_or_zero(src + r * n + e_ch, ok);
+      oa[u] = ld_or_zero(src + r * n + o_ch, ok);
+    }
+    for (i64 row0 = R - 1; row0 >= 0; row0 -= U) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const i64 row = row0 - u;
+        if (row >= 0) {
+          T v = T(0);
+          if (row + d < R) {
+            v = add_rn(v, oa[u]);
+            v = sub_rn(v, ea[u]);
+          }
+          if (row + 1 < R) v = add_rn(v, prev);
+          dst[row * n + ch] = v;
+          prev = v;
+        }
+        const i64 r = row - U + d;
+        const bool ok = r < R && r >= d;
+        ea[u] = ld_or_zero(src + r * n + e_ch, ok);
+        oa[u] = ld_or_zero(src + r * n + o_ch, ok);
       }
-      if (row + 1 < R) v = add_rn(v, prev);
-      dst[row * n + ch] = v;
-      prev = v;
     }
   }
 }

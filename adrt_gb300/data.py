@@ -59,3 +59,19 @@ def mixed_batch(batch: int, n: int, seed: int = 0, device="cuda", dtype=torch.fl
     x[:h] = uniform_images(h, n, seed, device, dtype)
     x[h:] = ellipse_phantoms(batch - h, n, seed + 100_000, device, dtype)
     return x
+
+
+RAGGED_SIZES = (32, 64, 128, 256, 512, 1024)
+RAGGED_WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.07, 0.03)
+
+
+def ragged_sizes(count: int, seed: int = 0):
+    """Image sides of the ragged workload: N drawn from {32, ..., 1024} with
+    weights {.3, .25, .2, .15, .07, .03}."""
+    rng = np.random.default_rng(seed)
+    return [int(v) for v in rng.choice(RAGGED_SIZES, size=count, p=RAGGED_WEIGHTS)]
+
+
+def ragged_phantoms(count: int, seed: int = 0, device="cuda", dtype=torch.float32):
+    """A list of `count` ellipse phantoms with sides from ragged_sizes."""
+    return [ellipse_phantoms(1, n, seed + i, device, dtype)[0] for i, n in enumerate(ragged_sizes(count, seed))]
