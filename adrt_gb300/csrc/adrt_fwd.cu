@@ -51,16 +51,23 @@ struct FwdPassArgs {
   i64 cs_out = 0;  // row stride of a non-final output buffer (0: 2n-1)
 };
 
-// Shared-memory rows of one tile.  During a stage each thread owns one output
-// row and every lanes-per-row'th position of it; the row stride is padded so
-// that the rows a warp covers start in different banks.
-template <int ROWS, int W>
+// Shared-memory rows of one tile.  During a stage a row is swept by TPR
+// consecutive threads (a whole warp, or several warps for few rows), so stage
+// accesses never conflict.  The transposing accesses (first-pass loads of
+// quadrants 1 and 2, last-pass stores) have consecutive threads on
+// consecutive rows: the row stride is TWP (a multiple of 32) plus PAD, chosen
+// so that the rows and positions one shared-memory wavefront covers (32 lanes
+// of 4-byte, 16 of 8-byte elements) fall in distinct banks.
+template <typename T, int ROWS, int W>
 struct FwdTile {
-  static constexpr int TWP = W + kFwdHalo;              // positions per row
-  static constexpr int LPR = kFwdThreads / ROWS;        // threads per row
-  static constexpr int RPW = LPR >= 32 ? 1 : 32 / LPR;  // rows per warp
-  static constexpr int RS = TWP + (RPW > 1 ? 32 / RPW : 0);
+  static constexpr int TWP = W + kFwdHalo;                  // positions per row
+  static constexpr int WF = sizeof(T) == 4 ? 32 : 16;       // lanes per wavefront
+  static constexpr int PAD = ROWS == 1 ? 0 : (ROWS >= WF ? 1 : WF / ROWS);
+  static constexpr int RS = TWP + PAD;
   static constexpr int BUF = ROWS * RS;
+  static constexpr int TPR = ROWS >= 8 ? 32 : kFwdThreads / ROWS;  // threads per row
+  static constexpr int ROW_STEP = kFwdThreads / TPR;               // rows in flight
+  static_assert(TWP % 32 == 0, "tile width plus halo must be a multiple of 32");
 };
 
 // Loads for non-first passes go through L2 only (the ragged kernel reads
@@ -74,7 +81,7 @@ template <typename T, int S, bool FIRST, bool LAST, int kFwdW>
 __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
                                          unsigned char *smem_raw) {
   constexpr int ROWS = 1 << S;
-  using TL = FwdTile<ROWS, kFwdW>;
+  using TL = FwdTile<T, ROWS, kFwdW>;
   constexpr int TWP = TL::TWP, RS = TL::RS;
   T *buf0 = reinterpret_cast<T *>(smem_raw);
   T *buf1 = buf0 + TL::BUF;
@@ -139,16 +146,18 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   // ---- S stages in shared memory: row m*2A + 2li + p of the output is
   // row 2m*A + li plus row (2m+1)*A + li shifted by li + p.
   T *cur = buf0, *nxt = buf1;
-  const int rowo = threadIdx.x / TL::LPR, lr = threadIdx.x % TL::LPR;
+  const int lr = threadIdx.x % TL::TPR;
 #pragma unroll
   for (int j = 0; j < S; ++j) {
     const int Al_in = 1 << j, Al_out = 2 << j;
-    const int m = rowo / Al_out, lo = rowo % Al_out;
-    const int li = lo >> 1, sh = li + (lo & 1);
-    const T *ep = cur + ((2 * m) * Al_in + li) * RS;
-    const T *op = cur + ((2 * m + 1) * Al_in + li) * RS - sh;  // row index >= 1, so in bounds
-    T *np = nxt + rowo * RS;
-    for (int u = lr; u < TWP; u += TL::LPR) np[u] = add_rn(ep[u], op[u]);
+    for (int rowo = threadIdx.x / TL::TPR; rowo < ROWS; rowo += TL::ROW_STEP) {
+      const int m = rowo / Al_out, lo = rowo % Al_out;
+      const int li = lo >> 1, sh = li + (lo & 1);
+      const T *ep = cur + ((2 * m) * Al_in + li) * RS;
+      const T *op = cur + ((2 * m + 1) * Al_in + li) * RS - sh;  // row index >= 1, so in bounds
+      T *np = nxt + rowo * RS;
+      for (int u = lr; u < TWP; u += TL::TPR) np[u] = add_rn(ep[u], op[u]);
+    }
     __syncthreads();
     T *tmp = cur; cur = nxt; nxt = tmp;
   }
@@ -195,7 +204,7 @@ static int plan_passes(int L, int *sizes, int max_fused = 5) { return plan_stage
 template <typename T, int S, bool FIRST, bool LAST, int W>
 static int launch_fwd_pass_w(const FwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S;
-  const size_t smem = 2 * sizeof(T) * FwdTile<ROWS, W>::BUF;
+  const size_t smem = 2 * sizeof(T) * FwdTile<T, ROWS, W>::BUF;
   auto kern = fwd_pass_kernel<T, S, FIRST, LAST, W>;
   static bool configured = false;  // per-instantiation, host-side only
   if (!configured) {
@@ -511,7 +520,7 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
       cudaMemsetAsync(base + p.off_ctl, 0, sizeof(unsigned) * (size_t)(2 + count), st) != cudaSuccess)
     return ADRT_GB300_ERR_CUDA;
   // The copies above are from pageable memory: they complete before the calls return.
-  constexpr size_t smem = 2 * sizeof(T) * FwdTile<32, kFwdWNarrow>::BUF;
+  constexpr size_t smem = 2 * sizeof(T) * FwdTile<T, 32, kFwdWNarrow>::BUF;
   auto kern = ragged_fwd_kernel<T>;
   static bool configured = false;
   if (!configured) {

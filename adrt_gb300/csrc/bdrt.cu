@@ -39,22 +39,28 @@ struct BwdPassArgs {
 // Buffer layout between passes, per (b, q): [angle s][section p][offset c],
 // the reference's bdrt buffer.  After forward stage k0 there are A = 2^k0
 // angles and R = n / 2^k0 sections.
-// Shared-memory rows of one tile (same thread mapping as the forward kernel);
-// a 32-element tail pad keeps the right-shifted reads of the last row in bounds.
-template <int ROWS>
+// Shared-memory rows of one tile, with the forward kernel's layout rules: a
+// stage sweeps each row with TPR consecutive threads, and the row stride is
+// padded so the transposing first-pass loads and last-pass stores hit
+// distinct banks.  A 32-element tail pad keeps the right-shifted reads of the
+// last row in bounds.
+template <typename T, int ROWS>
 struct BwdTile {
   static constexpr int TWP = kBwdW + kBwdHalo;
-  static constexpr int LPR = kBwdThreads / ROWS;
-  static constexpr int RPW = LPR >= 32 ? 1 : 32 / LPR;
-  static constexpr int RS = TWP + (RPW > 1 ? 32 / RPW : 0);
+  static constexpr int WF = sizeof(T) == 4 ? 32 : 16;  // lanes per wavefront
+  static constexpr int PAD = ROWS == 1 ? 0 : (ROWS >= WF ? 1 : WF / ROWS);
+  static constexpr int RS = TWP + PAD;
   static constexpr int BUF = ROWS * RS + 32;
+  static constexpr int TPR = ROWS >= 8 ? 32 : kBwdThreads / ROWS;
+  static constexpr int ROW_STEP = kBwdThreads / TPR;
+  static_assert(TWP % 32 == 0, "tile width plus halo must be a multiple of 32");
 };
 
 template <typename T, int S, bool FIRST, bool LAST>
 __global__ void __launch_bounds__(kBwdThreads)
 bwd_pass_kernel(BwdPassArgs args) {
   constexpr int ROWS = 1 << S;
-  using TL = BwdTile<ROWS>;
+  using TL = BwdTile<T, ROWS>;
   constexpr int TWP = TL::TWP, RS = TL::RS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf0 = reinterpret_cast<T *>(smem_raw);
@@ -109,29 +115,31 @@ bwd_pass_kernel(BwdPassArgs args) {
   // Level j+1 buffer rows: combo m, local angle la -> row m * 2^(j+1) + la.
   // Level j buffer rows:   combo m', local angle li -> row m' * 2^j + li.
   T *cur = buf0, *nxt = buf1;
-  const int rowo = threadIdx.x / TL::LPR, lr = threadIdx.x % TL::LPR;
+  const int lr = threadIdx.x % TL::TPR;
 #pragma unroll
   for (int j = S - 1; j >= 0; --j) {
     const int Al_hi = 2 << j;          // local angles at level j+1
     const int Al_lo = 1 << j;          // local angles at level j
-    const int mm = rowo / Al_lo, li = rowo % Al_lo;  // level-j combo, angle
-    const int m = mm >> 1;                           // parent combo at level j+1
-    const T *ya = cur + (m * Al_hi + 2 * li) * RS;
-    const T *yb = ya + RS;
-    T *np = nxt + rowo * RS;
-    if ((mm & 1) == 0) {
-      // left: la + lb (positions past the buffer end are never used)
-      for (int u = lr; u < TWP; u += TL::LPR) np[u] = add_rn(ya[u], yb[u]);
-    } else {
-      // right: reference offset of la is base + u, with the parent mapping a'*2m*2^j.
-      const i64 base = c0 + li - ap * (i64)((2 * m) << j);
-      const i64 last_add = C - 2 - base;  // u <= last_add: la + lbb
-      for (int u = lr; u < TWP; u += TL::LPR) {
-        T v;
-        if (u <= last_add) v = add_rn(ya[u + li], yb[u + li + 1]);
-        else if (u == last_add + 1) v = ya[u + li];  // copy of la at offset C-1
-        else v = T(0);
-        np[u] = v;
+    for (int rowo = threadIdx.x / TL::TPR; rowo < ROWS; rowo += TL::ROW_STEP) {
+      const int mm = rowo / Al_lo, li = rowo % Al_lo;  // level-j combo, angle
+      const int m = mm >> 1;                           // parent combo at level j+1
+      const T *ya = cur + (m * Al_hi + 2 * li) * RS;
+      const T *yb = ya + RS;
+      T *np = nxt + rowo * RS;
+      if ((mm & 1) == 0) {
+        // left: la + lb (positions past the buffer end are never used)
+        for (int u = lr; u < TWP; u += TL::TPR) np[u] = add_rn(ya[u], yb[u]);
+      } else {
+        // right: reference offset of la is base + u, with the parent mapping a'*2m*2^j.
+        const i64 base = c0 + li - ap * (i64)((2 * m) << j);
+        const i64 last_add = C - 2 - base;  // u <= last_add: la + lbb
+        for (int u = lr; u < TWP; u += TL::TPR) {
+          T v;
+          if (u <= last_add) v = add_rn(ya[u + li], yb[u + li + 1]);
+          else if (u == last_add + 1) v = ya[u + li];  // copy of la at offset C-1
+          else v = T(0);
+          np[u] = v;
+        }
       }
     }
     __syncthreads();
@@ -166,7 +174,7 @@ static int plan_passes_bwd(i64 n, size_t elem, int *sizes) {
 template <typename T, int S, bool FIRST, bool LAST>
 static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S;
-  const size_t smem = 2 * sizeof(T) * BwdTile<ROWS>::BUF;
+  const size_t smem = 2 * sizeof(T) * BwdTile<T, ROWS>::BUF;
   auto kern = bwd_pass_kernel<T, S, FIRST, LAST>;
   static bool configured = false;
   if (!configured) {
