@@ -97,7 +97,7 @@ def test_oracle_large(oracle_mod, dt, n, b):
     yz[:, :, -5:] = -0.0
     z = adrt.bdrt(dev(yz))
     assert bits_equal(host(z), oracle_mod.bdrt(yz))
-    if n <= 256:
+    if n <= 1024:
         inv = adrt.iadrt(dev(want))
         assert bits_equal(host(inv), oracle_mod.iadrt(want))
 
