@@ -57,6 +57,11 @@ SIGNATURES = {
     "adrt_gb300_adrt_init": [_v, _v, _i64, _i64, _sz, _v],
     "adrt_gb300_truncate": [_v, _v, _i64, _i64, _sz, _v],
     "adrt_gb300_stitch": [_v, _v, _i64, _i64, _int, _sz, _v],
+    "adrt_gb300_unstitch": [_v, _v, _i64, _i64, _int, _sz, _v],
+    "adrt_gb300_interp_to_cart": [_v, _v, _i64, _i64, _int, _v],
+    "adrt_gb300_interp_table": [_i64, _v, _v, _v],
+    "adrt_gb300_coord_adrt": [_i64, _v, _v, _v],
+    "adrt_gb300_coord_cart_to_adrt": [_v, _v, _i64, _i64, _int, _v, _v, _v, _v, _v],
     "adrt_gb300_fmg_restriction": [_v, _v, _i64, _i64, _int, _v],
     "adrt_gb300_fmg_prolongation": [_v, _v, _i64, _i64, _i64, _int, _v],
     "adrt_gb300_fmg_highpass": [_v, _v, _i64, _i64, _i64, _int, _v],
@@ -72,6 +77,7 @@ SIGNATURES = {
     "adrt_gb300_batched_dot": [_v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
+    "adrt_gb300_axpy": [ctypes.c_double, _v, _v, _i64, _int, _v],
     "adrt_gb300_tune_set": [_int, _int, _i64, _int, _int, _int, _int],
     "adrt_gb300_tune_get": [_int, _int, _i64, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int),
                             ctypes.POINTER(_int)],

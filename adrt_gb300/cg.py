@@ -6,8 +6,13 @@ reconstruction recipe the reference documents with SciPy
 (docs/examples.cginverse.md:40-67, operator truncate(bdrt(adrt(x))).mean(0));
 the mean there is 1/4 of A^T, which leaves the solution unchanged.
 
+With ``ridge_param`` = lambda > 0 the operator is the reference's
+``ADRTRidgeOperator`` (docs/examples.tomography.md:63-76): its normal
+operator is the quadrant *mean* plus lambda I, so the system solved is
+(A^T A / 4 + lambda I) x = A^T b / 4, i.e. (A^T A + 4 lambda I) x = A^T b.
+
 Each image stops when its normal-equation residual
-||A^T(A x - b)|| / ||A^T b|| <= tol (the quantity CG on A^T A controls); the
+||A^T b - (A^T A + 4 lambda I) x|| / ||A^T b|| <= tol (the quantity CG controls); the
 batch runs until all images stopped or `max_iters`.  All vector algebra runs
 in the library's CG kernels with float64 per-image scalars; with
 ``graph=True`` one CG iteration is captured in a CUDA graph and replayed.
@@ -27,9 +32,14 @@ from ._wrappers import float_code
 __all__ = ["normal_op", "cg", "CGResult"]
 
 
-def normal_op(x: torch.Tensor) -> torch.Tensor:
-    """A^T A x for a batch of images on the device."""
-    return _adjoint(_adrt(x))
+def normal_op(x: torch.Tensor, lam: float = 0.0) -> torch.Tensor:
+    """(A^T A + lam I) x for a batch of images on the device."""
+    y = _adjoint(_adrt(x))
+    if lam:
+        rc = _lib.load().adrt_gb300_axpy(float(lam), x.data_ptr(), y.data_ptr(), x.numel(), float_code(x),
+                                         torch.cuda.current_stream(x.device).cuda_stream)
+        _lib.check(rc, "axpy")
+    return y
 
 
 @dataclass
@@ -42,7 +52,8 @@ class CGResult:
 
 
 class _State:
-    def __init__(self, b, x0):
+    def __init__(self, b, x0, lam=0.0):
+        self.lam = lam
         self.dev = b.device
         self.B = b.shape[0]
         n = b.shape[-1]
@@ -50,7 +61,7 @@ class _State:
         self.code = float_code(b)
         self.x = torch.zeros((self.B, n, n), dtype=b.dtype, device=b.device) if x0 is None else x0.clone().contiguous()
         self.rhs = _adjoint(b.contiguous())
-        self.r = self.rhs - normal_op(self.x) if x0 is not None else self.rhs.clone()
+        self.r = self.rhs - normal_op(self.x, lam) if x0 is not None else self.rhs.clone()
         self.p = self.r.clone()
         self.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(self.B), dtype=torch.uint8, device=b.device)
         self.rs = self.dot(self.r, self.r)
@@ -72,7 +83,7 @@ class _State:
 
     def iterate(self, thr2):
         lib = _lib.load()
-        Ap = normal_op(self.p)
+        Ap = normal_op(self.p, self.lam)
         rc = lib.adrt_gb300_batched_dot(self.p.data_ptr(), Ap.data_ptr(), self.pAp.data_ptr(), self.B,
                                         self.per, self.code, self.ws.data_ptr(), self.stream())
         _lib.check(rc, "batched_dot")
@@ -91,11 +102,14 @@ class _State:
 
 
 def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, max_iters: int = 1000,
-       check_every: int = 4, graph: bool = False) -> CGResult:
-    """Batched CG for A^T A x = A^T b; b: CUDA tensor (B, 4, 2n-1, n)."""
+       check_every: int = 4, graph: bool = False, ridge_param: float = 0.0) -> CGResult:
+    """Batched CG for (A^T A + 4 ridge_param I) x = A^T b; b: CUDA tensor
+    (B, 4, 2n-1, n)."""
     if not (isinstance(b, torch.Tensor) and b.is_cuda and b.ndim == 4):
         raise TypeError("cg expects a CUDA tensor of shape (B, 4, 2n-1, n)")
-    st = _State(b, x0)
+    if ridge_param < 0:
+        raise ValueError("ridge_param must be non-negative")
+    st = _State(b, x0, 4.0 * float(ridge_param))
     thr2 = st.rhs2 * (tol * tol)
     st.active.copy_((st.rs > thr2).to(torch.int32))
     k = 0
@@ -122,7 +136,7 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
         if not bool(st.active.any().item()):
             break
     # Recompute the reported residuals from scratch.
-    res_n = normal_op(st.x) - st.rhs
+    res_n = normal_op(st.x, st.lam) - st.rhs
     ax = _adrt(st.x)
     dr = ax - b
     normal_residual = torch.sqrt(st.dot(res_n, res_n) / st.rhs2)

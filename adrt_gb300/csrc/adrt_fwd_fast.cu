@@ -36,7 +36,6 @@ constexpr int NCH = TW / 4;       // 128 chunks of 4 positions
 constexpr int RS = 4 * (NCH + 1); // exchange row stride in floats (odd chunk count)
 constexpr int NT = 256;           // threads per CTA
 constexpr int N = 1024;
-constexpr int C = 2 * N - 1;
 // After five stages a row group's values are non-zero only at offsets below
 // n + 31 (shifts reach 31); beyond that every value is +0, the sum of the
 // zero padding.  Pass A computes the tiles that hold those offsets and the

@@ -29,12 +29,14 @@ int cg_update_launch(T *, T *, const T *, const T *, const double *, const doubl
                      double *, i64, i64, void *, cudaStream_t);
 template <typename T>
 int cg_direction_launch(T *, const T *, const double *, double *, const int *, i64, i64, cudaStream_t);
+template <typename T> int axpy_launch(double, const T *, T *, i64, cudaStream_t);
 size_t fwd_workspace_bytes(i64, i64, size_t);
 size_t bwd_workspace_bytes(i64, i64, size_t);
 size_t iadrt_workspace_bytes(i64, i64, size_t);
 int init_launch(const void *, void *, i64, i64, size_t, cudaStream_t);
 int truncate_launch(const void *, void *, i64, i64, size_t, cudaStream_t);
 int stitch_launch(const void *, void *, i64, i64, int, size_t, cudaStream_t);
+int unstitch_launch(const void *in, void *out, i64 batch, i64 n, i64 vc, size_t es, cudaStream_t st);
 }  // namespace adrtg
 
 #include <atomic>
@@ -205,6 +207,13 @@ int adrt_gb300_stitch(const void *in, void *out, int64_t batch, int64_t n, int r
   return stitch_launch(in, out, batch, n, remove_repeated ? 1 : 0, es, S(stream));
 }
 
+int adrt_gb300_unstitch(const void *in, void *out, int64_t batch, int64_t n, int remove_repeated,
+                        size_t es, void *stream) {
+  if (!in || !out) return ADRT_GB300_ERR_NULL;
+  if (batch < 1 || n < 1) return ADRT_GB300_ERR_SHAPE;
+  return unstitch_launch(in, out, batch, n, n - (remove_repeated ? 1 : 0), es, S(stream));
+}
+
 int adrt_gb300_fmg_restriction(const void *in, void *out, int64_t batch, int64_t n, int dtype,
                                void *stream) {
   int rc;
@@ -314,6 +323,16 @@ int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double
   return DISPATCH(dtype,
                   cg_direction_launch<float>((float *)p, (const float *)r, rs_new, rs, active, batch, per, S(stream)),
                   cg_direction_launch<double>((double *)p, (const double *)r, rs_new, rs, active, batch, per, S(stream)));
+}
+
+int adrt_gb300_axpy(double alpha, const void *x, void *y, int64_t count, int dtype, void *stream) {
+  int rc;
+  if (!x || !y) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (count < 0) return ADRT_GB300_ERR_SHAPE;
+  if (count == 0) return ADRT_GB300_OK;
+  return DISPATCH(dtype, axpy_launch<float>(alpha, (const float *)x, (float *)y, count, S(stream)),
+                  axpy_launch<double>(alpha, (const double *)x, (double *)y, count, S(stream)));
 }
 
 }  // extern "C"

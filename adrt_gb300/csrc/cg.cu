@@ -125,12 +125,27 @@ int cg_direction_launch(T *p, const T *r, const double *rs_new, double *rs, cons
   return launch_status();
 }
 
+// y += alpha * x (one rounding for the product, one for the sum; no FMA).
+template <typename T>
+__global__ void axpy_kernel(T alpha, const T *__restrict__ x, T *__restrict__ y, i64 count) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < count; i += (i64)gridDim.x * blockDim.x)
+    y[i] = add_rn(y[i], mul_rn(alpha, x[i]));
+}
+
+template <typename T>
+int axpy_launch(double alpha, const T *x, T *y, i64 count, cudaStream_t st) {
+  const i64 blocks = (count + 255) / 256;
+  axpy_kernel<T><<<(unsigned)(blocks < 8192 ? blocks : 8192), 256, 0, st>>>((T)alpha, x, y, count);
+  return launch_status();
+}
+
 #define INST(T)                                                                                \
   template int batched_dot_launch<T>(const T *, const T *, double *, i64, i64, void *, cudaStream_t); \
   template int cg_update_launch<T>(T *, T *, const T *, const T *, const double *, const double *, \
                                    const int *, double *, i64, i64, void *, cudaStream_t);     \
   template int cg_direction_launch<T>(T *, const T *, const double *, double *, const int *, i64, \
-                                      i64, cudaStream_t);
+                                      i64, cudaStream_t);                                      \
+  template int axpy_launch<T>(double, const T *, T *, i64, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

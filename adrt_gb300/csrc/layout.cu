@@ -94,6 +94,34 @@ __global__ void stitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64
   }
 }
 
+// (3n-2, 4, vc) -> (4, 2n-1, n), the inverse of stitch_kernel: quadrant q
+// read from rows [0, 2n-1) (q < 2) or [n-1, 3n-2) (q >= 2), flipped on both
+// axes when q is odd; with vc = n-1 the last column comes from column 0 of
+// quadrant q+1 (rows reversed for q = 3).  Reference: src/adrt/utils.py:137-188.
+template <typename W>
+__global__ void unstitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n, i64 vc) {
+  const i64 C = 2 * n - 1, OR = 3 * n - 2;
+  const i64 total = batch * 4 * C * n;
+  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
+       idx += (i64)gridDim.x * blockDim.x) {
+    const i64 c = idx % n;
+    const i64 r = (idx / n) % C;
+    const int q = (int)((idx / (n * C)) % 4);
+    const i64 b = idx / (4 * C * n);
+    const i64 rs = (q & 1) ? C - 1 - r : r;
+    const i64 cs = (q & 1) ? n - 1 - c : c;
+    const i64 R = rs + (q >= 2 ? n - 1 : 0);
+    i64 src;
+    if (cs < vc) {
+      src = ((b * OR + R) * 4 + q) * vc + cs;
+    } else {
+      const i64 R2 = q == 3 ? OR - 1 - R : R;
+      src = ((b * OR + R2) * 4 + (q + 1) % 4) * vc;
+    }
+    out[idx] = in[src];
+  }
+}
+
 // Adjoint tail: out[b][i][j] = ((t0 + t1) + t2) + t3 with t_q = truncate(y)[q].
 template <typename T>
 __global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, i64 batch, i64 n) {
@@ -143,6 +171,11 @@ int truncate_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cuda
 
 int stitch_launch(const void *in, void *out, i64 batch, i64 n, int rr, size_t es, cudaStream_t st) {
   BY_SIZE(es, stitch_kernel, batch * (3 * n - 2) * 4 * n, batch, n, rr)
+  return launch_status();
+}
+
+int unstitch_launch(const void *in, void *out, i64 batch, i64 n, i64 vc, size_t es, cudaStream_t st) {
+  BY_SIZE(es, unstitch_kernel, batch * 4 * (2 * n - 1) * n, batch, n, vc)
   return launch_status();
 }
 

@@ -179,6 +179,44 @@ int adrt_gb300_truncate(const void *in, void *out, int64_t batch, int64_t n,
 int adrt_gb300_stitch(const void *in, void *out, int64_t batch, int64_t n,
                       int remove_repeated, size_t elem_size, void *stream);
 
+/* Unstitch, the inverse of stitch: (batch, 3n-2, 4*(n - remove_repeated)) ->
+ * (batch, 4, 2n-1, n); with remove_repeated each quadrant's last column is
+ * taken from the next quadrant's first.  Any element type.  Replaces
+ * adrt.utils.unstitch_adrt (src/adrt/utils.py:137-188). */
+int adrt_gb300_unstitch(const void *in, void *out, int64_t batch, int64_t n,
+                        int remove_repeated, size_t elem_size, void *stream);
+
+/* interp_to_cart: (batch, 4, 2n-1, n) -> (batch, n, 4n), n a power of two
+ * >= 2, float32/float64.  Replaces adrt::interp_adrtcart
+ * (src/adrt/adrt_cdefs_interp_adrtcart.hpp:62-114), bound as
+ * _adrt_cdefs.interp_to_cart with a float index type
+ * (src/adrt/adrt_cdefs_py.cpp:621-682).  The first call for a given n on a
+ * device builds and keeps that size's index table (host arithmetic and a
+ * device allocation): do not make that first call inside CUDA-graph capture.
+ * ADRT_GB300_ERR_TOO_LARGE when 4n exceeds the float index range. */
+int adrt_gb300_interp_to_cart(const void *in, void *out, int64_t batch, int64_t n, int dtype, void *stream);
+
+/* Host-only: the selection table behind interp_to_cart for size n, into
+ * host buffers idx[n * 4n] (offset of the selected entry within one image's
+ * (4, 2n-1, n) array, or -1 where the output is zero), fac32[4n] and
+ * fac64[4n] (the scale factor per output column for float32 / float64 data).
+ * out[b][o][a] = fac[a] * in[b][idx[o][a]].  No device work. */
+int adrt_gb300_interp_table(int64_t n, int32_t *idx, float *fac32, double *fac64);
+
+/* coord_adrt: the Radon offset (4, 2n-1, n) and angle (4, 1, n) of every
+ * ADRT entry, float64, n a power of two >= 2.  Replaces adrt.utils.coord_adrt
+ * (src/adrt/utils.py:250-332, NumPy code); arctan/sin/cos may differ from
+ * NumPy's in the last place. */
+int adrt_gb300_coord_adrt(int64_t n, double *offset, double *angle, void *stream);
+
+/* coord_cart_to_adrt: for `count` points (theta, t) of dtype F32/F64, the
+ * nearest ADRT entry (quadrant uint8, height int64, slope uint64) and its
+ * scale factor (float64).  Replaces adrt.utils.coord_cart_to_adrt
+ * (src/adrt/utils.py:335-435), following NumPy's dtypes and rounding. */
+int adrt_gb300_coord_cart_to_adrt(const void *theta, const void *t, int64_t count, int64_t n, int dtype,
+                                  uint8_t *quadrant, int64_t *height, uint64_t *slope, double *factor,
+                                  void *stream);
+
 /* Multigrid restriction: (batch, 4, 2n-1, n) -> (batch, 4, n-1, n/2), n even.
  * Replaces adrt::fmg_restriction (src/adrt/adrt_cdefs_fmg.hpp:53-73),
  * bound as _adrt_cdefs.press_fmg_restriction (src/adrt/adrt_cdefs_py.cpp:684-738). */
@@ -243,6 +281,11 @@ int adrt_gb300_cg_update(void *x, void *r, const void *p, const void *Ap, const 
 /* beta_i = rs_new[i] / rs[i]; p = r + beta p; rs[i] = rs_new[i]. */
 int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double *rs,
                             const int *active, int64_t batch, int64_t per, int dtype, void *stream);
+
+/* y += alpha * x elementwise (alpha rounded to the dtype; product and sum
+ * rounded separately).  The ridge term of the regularised normal operator
+ * (A^T A + lambda I) x of docs/examples.tomography.md:63-76. */
+int adrt_gb300_axpy(double alpha, const void *x, void *y, int64_t count, int dtype, void *stream);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "golden.npz")
+GOLDEN_NEXT = os.path.join(ROOT, "tests", "golden", "golden_next.npz")
 
 
 def pytest_configure(config):
@@ -18,6 +19,12 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def golden():
     with np.load(GOLDEN) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def golden_next():
+    with np.load(GOLDEN_NEXT) as z:
         return {k: z[k] for k in z.files}
 
 

@@ -84,3 +84,36 @@ def test_graphed_forward_matches_eager():
         torch.manual_seed(seed)
         xn = torch.rand((2, 1024, 1024), device="cuda")
         assert torch.equal(g(xn), adrt.adrt(xn))
+
+
+def scipy_ridge_cg(oracle_mod, b, ridge_param, tol):
+    """The reference's ADRTRidgeOperator recipe (docs/examples.tomography.md:
+    63-76) on the oracle operator in float64."""
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    n = b.shape[-1]
+
+    def mv(v):
+        img = v.reshape(n, n)
+        return (oracle_mod.adjoint(oracle_mod.adrt(img)) / 4 + ridge_param * img).ravel()
+
+    op = sla.LinearOperator((n * n, n * n), matvec=mv, dtype=np.float64)
+    rhs = (oracle_mod.adjoint(b) / 4).ravel()
+    x, info = sla.cg(op, rhs, rtol=tol, maxiter=5000)
+    assert info == 0
+    return x.reshape(n, n)
+
+
+@pytest.mark.parametrize("ridge_param", [0.5, 20.0])
+def test_ridge_matches_scipy_oracle(oracle_mod, ridge_param):
+    n = 32
+    xt = ellipse_phantoms(2, n, seed=41, device="cuda", dtype=torch.float64)
+    b = adrt.adrt(xt)
+    res = cgmod.cg(b, tol=1e-11, max_iters=2000, ridge_param=ridge_param)
+    for i in range(2):
+        want = scipy_ridge_cg(oracle_mod, b[i].cpu().numpy(), ridge_param, 1e-13)
+        got = res.x[i].cpu().numpy()
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-8
+    plain = cgmod.cg(b, tol=1e-11, max_iters=2000)
+    # The ridge term shrinks the solution.
+    assert (res.x.norm(dim=(1, 2)) < plain.x.norm(dim=(1, 2))).all()
+    assert (res.normal_residual <= 1e-10).all()
