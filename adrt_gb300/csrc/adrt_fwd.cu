@@ -96,11 +96,13 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   const int col_tiles = (int)((C + kFwdW - 1) / kFwdW);
 
   // Decode the tile: (b, q, r, a', column tile), column tile fastest.
-  i64 t = tile;
-  const int ct = (int)(t % col_tiles); t /= col_tiles;
-  const i64 ap = t % A_in; t /= A_in;
-  const i64 r = t % R_out; t /= R_out;
-  const int q = (int)(t % 4); t /= 4;
+  // 32-bit decode: tile indices fit in 32 bits, and 64-bit division is a
+  // long instruction sequence that small tiles cannot amortise.
+  unsigned t = (unsigned)tile;
+  const int ct = (int)(t % (unsigned)col_tiles); t /= (unsigned)col_tiles;
+  const i64 ap = t % (unsigned)A_in; t /= (unsigned)A_in;
+  const i64 r = t % (unsigned)R_out; t /= (unsigned)R_out;
+  const int q = (int)(t & 3u); t >>= 2;
   const i64 b = t;
   const i64 c0 = (i64)ct * kFwdW;
   const i64 tbase = c0 - kFwdHalo;  // reference offset of tile position 0 (before pre-shift)

@@ -77,11 +77,12 @@ bwd_pass_kernel(BwdPassArgs args) {
   const i64 max_ext = (A_lo - 1) * (ROWS - 1);
   const int col_tiles = (int)((C + max_ext + kBwdW - 1) / kBwdW);
 
-  i64 t = blockIdx.x;
-  const int ct = (int)(t % col_tiles); t /= col_tiles;
-  const i64 ap = t % A_lo; t /= A_lo;
-  const i64 r = t % R_hi; t /= R_hi;
-  const int q = (int)(t % 4); t /= 4;
+  // 32-bit decode (64-bit division is a long instruction sequence).
+  unsigned t = blockIdx.x;
+  const int ct = (int)(t % (unsigned)col_tiles); t /= (unsigned)col_tiles;
+  const i64 ap = t % (unsigned)A_lo; t /= (unsigned)A_lo;
+  const i64 r = t % (unsigned)R_hi; t /= (unsigned)R_hi;
+  const int q = (int)(t & 3u); t >>= 2;
   const i64 b = t;
   const i64 c0 = (i64)ct * kBwdW;
   // Skip tiles that hold no member's needed offsets (member i of this tile

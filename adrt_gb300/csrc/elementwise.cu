@@ -17,15 +17,15 @@ __device__ __forceinline__ i64 trunc_idx(int q, i64 i, i64 j, i64 n) {
 // out = np.mean(truncate(y) / (n - 1), axis=-3): each quadrant value is divided
 // by (n-1) (one rounding), the four are summed in quadrant order, then divided
 // by 4, exactly as NumPy evaluates the expression at src/adrt/core.py:328-329.
-template <typename T>
-__global__ void fmg_correction_kernel(const T *__restrict__ y, T *__restrict__ out, i64 batch,
-                                      i64 n, T divisor) {
-  const i64 C = 2 * n - 1;
-  const i64 total = batch * n * n;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 j = idx % n, i = (idx / n) % n;
-    const T *yb = y + (idx / (n * n)) * 4 * C * n;
+// Index arithmetic in I (32-bit unsigned when the sizes allow); n is a power
+// of two here (lg = log2 n), so the decomposition is shifts and masks.
+template <typename T, typename I>
+__global__ void fmg_correction_kernel(const T *__restrict__ y, T *__restrict__ out, I total, I n, int lg,
+                                      T divisor) {
+  const I C = 2 * n - 1;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+    const I j = idx & (n - 1), i = (idx >> lg) & (n - 1);
+    const T *yb = y + (idx >> (2 * lg)) * 4 * C * n;
     T s = add_rn(div_rn(yb[trunc_idx(0, i, j, n)], divisor),
                  div_rn(yb[C * n + trunc_idx(1, i, j, n)], divisor));
     s = add_rn(s, div_rn(yb[2 * C * n + trunc_idx(2, i, j, n)], divisor));
@@ -84,7 +84,14 @@ static unsigned grid_e(i64 total) {
 
 template <typename T>
 int fmg_correction_launch(const T *y, T *out, i64 batch, i64 n, cudaStream_t st) {
-  fmg_correction_kernel<T><<<grid_e(batch * n * n), 256, 0, st>>>(y, out, batch, n, T(n - 1));
+  const i64 total = batch * n * n;
+  const int lg = num_iters(n);
+  if (total * 8 < (i64(1) << 32))
+    fmg_correction_kernel<T, unsigned><<<grid_e(total), 256, 0, st>>>(y, out, (unsigned)total, (unsigned)n, lg,
+                                                                      T(n - 1));
+  else
+    fmg_correction_kernel<T, unsigned long long><<<grid_e(total), 256, 0, st>>>(
+        y, out, (unsigned long long)total, (unsigned long long)n, lg, T(n - 1));
   return launch_status();
 }
 

@@ -123,15 +123,15 @@ __global__ void unstitch_kernel(const W *__restrict__ in, W *__restrict__ out, i
 }
 
 // Adjoint tail: out[b][i][j] = ((t0 + t1) + t2) + t3 with t_q = truncate(y)[q].
-template <typename T>
-__global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, i64 batch, i64 n) {
-  const i64 C = 2 * n - 1;
-  const i64 total = batch * n * n;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 j = idx % n;
-    const i64 i = (idx / n) % n;
-    const T *yb = y + (idx / (n * n)) * 4 * C * n;
+// n is a power of two (lg = log2 n): index arithmetic is shifts and masks, in
+// 32-bit unsigned when the element count allows.
+template <typename T, typename I>
+__global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, I total, I n, int lg) {
+  const I C = 2 * n - 1;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+    const I j = idx & (n - 1);
+    const I i = (idx >> lg) & (n - 1);
+    const T *yb = y + (idx >> (2 * lg)) * 4 * C * n;
     T s = add_rn(yb[trunc_src(0, i, j, n)], yb[C * n + trunc_src(1, i, j, n)]);
     s = add_rn(s, yb[2 * C * n + trunc_src(2, i, j, n)]);
     out[idx] = add_rn(s, yb[3 * C * n + trunc_src(3, i, j, n)]);
@@ -181,7 +181,13 @@ int unstitch_launch(const void *in, void *out, i64 batch, i64 n, i64 vc, size_t 
 
 template <typename T>
 int quad_sum_launch(const T *y, T *out, i64 batch, i64 n, cudaStream_t st) {
-  quad_sum_kernel<T><<<grid_l(batch * n * n), 256, 0, st>>>(y, out, batch, n);
+  const i64 total = batch * n * n;
+  const int lg = num_iters(n);
+  if (total * 8 < (i64(1) << 32))
+    quad_sum_kernel<T, unsigned><<<grid_l(total), 256, 0, st>>>(y, out, (unsigned)total, (unsigned)n, lg);
+  else
+    quad_sum_kernel<T, unsigned long long><<<grid_l(total), 256, 0, st>>>(y, out, (unsigned long long)total,
+                                                                            (unsigned long long)n, lg);
   return launch_status();
 }
 template int quad_sum_launch<float>(const float *, float *, i64, i64, cudaStream_t);

@@ -8,23 +8,25 @@ namespace adrtg {
 // operand b at (row - ceil(angle/2), (2*block+1)*2^k + angle/2); copy of a
 // when row < ceil(angle/2).
 // Reference: src/adrt/adrt_cdefs_adrt.hpp:215-258 (adrt_step).
-template <typename T>
-__global__ void adrt_step_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes,
-                                 i64 n, int k) {
-  const i64 C = 2 * n - 1;
-  const i64 total = planes * C * n;
-  const i64 E = i64(1) << k;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 col = idx % n;
-    const i64 row = (idx / n) % C;
-    const i64 base = idx - row * n - col;  // start of this plane
-    const i64 blk = col >> (k + 1), ang = col & (2 * E - 1);
-    const i64 ca = 2 * blk * E + (ang >> 1);
-    const i64 cb = ca + E;
-    const i64 sh = (ang + 1) >> 1;
-    const T av = in[base + row * n + ca];
-    out[idx] = row >= sh ? add_rn(av, in[base + (row - sh) * n + cb]) : av;
+// Index arithmetic runs in I: 32-bit unsigned whenever the element count
+// allows (64-bit division is a long instruction sequence), 64-bit otherwise.
+// n is a power of two (lg = log2 n): the column is a mask, the row one
+// division by C = 2n-1.
+template <typename T, typename I>
+__global__ void adrt_step_kernel(const T *__restrict__ in, T *__restrict__ out, I total, I n, int lg, int k) {
+  const I C = 2 * n - 1;
+  const I E = I(1) << k;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+    const I col = idx & (n - 1);
+    const I rp = idx >> lg;  // plane * C + row
+    const I row = rp % C;
+    const I base = (rp - row) << lg;  // start of this plane
+    const I blk = col >> (k + 1), ang = col & (2 * E - 1);
+    const I ca = 2 * blk * E + (ang >> 1);
+    const I cb = ca + E;
+    const I sh = (ang + 1) >> 1;
+    const T av = in[base + (row << lg) + ca];
+    out[idx] = row >= sh ? add_rn(av, in[base + ((row - sh) << lg) + cb]) : av;
   }
 }
 
@@ -32,31 +34,32 @@ __global__ void adrt_step_kernel(const T *__restrict__ in, T *__restrict__ out, 
 // two neighbours in the same row; odd blocks add along the diagonal
 // (row+i, row+i+1), where a missing operand is +0 and is still added.
 // Reference: src/adrt/adrt_cdefs_bdrt.hpp:190-244 (bdrt_step).
-template <typename T>
-__global__ void bdrt_step_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes,
-                                 i64 n, int ek) {
-  const i64 C = 2 * n - 1;
-  const i64 total = planes * C * n;
-  const i64 E = i64(1) << ek;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 col = idx % n;
-    const i64 row = (idx / n) % C;
-    const i64 base = idx - row * n - col;
-    const i64 blk = col >> ek, i = col & (E - 1);
-    const i64 bc = 2 * (i + E * (blk >> 1));
+template <typename T, typename I>
+__global__ void bdrt_step_kernel(const T *__restrict__ in, T *__restrict__ out, I total, I n, int lg, int ek) {
+  const I C = 2 * n - 1;
+  const I E = I(1) << ek;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total; idx += (I)gridDim.x * blockDim.x) {
+    const I col = idx & (n - 1);
+    const I rp = idx >> lg;
+    const I row = rp % C;
+    const I base = (rp - row) << lg;
+    const I blk = col >> ek, i = col & (E - 1);
+    const I bc = 2 * (i + E * (blk >> 1));
     T v;
     if ((blk & 1) == 0) {
-      v = add_rn(in[base + row * n + bc], in[base + row * n + bc + 1]);
+      v = add_rn(in[base + (row << lg) + bc], in[base + (row << lg) + bc + 1]);
     } else {
-      const i64 r0 = row + i;
-      const T av = r0 < C ? in[base + r0 * n + bc] : T(0);
-      const T bv = r0 + 1 < C ? in[base + (r0 + 1) * n + bc + 1] : T(0);
+      const I r0 = row + i;
+      const T av = r0 < C ? in[base + (r0 << lg) + bc] : T(0);
+      const T bv = r0 + 1 < C ? in[base + ((r0 + 1) << lg) + bc + 1] : T(0);
       v = add_rn(av, bv);
     }
     out[idx] = v;
   }
 }
+
+// 32-bit indices when every index (plus one grid stride) stays below 2^32.
+inline bool fits_u32(i64 total) { return total < (i64(1) << 32) - (i64(1) << 24); }
 
 static unsigned grid_for(i64 total, int threads) {
   i64 g = (total + threads - 1) / threads;
@@ -69,7 +72,12 @@ static unsigned grid_for(i64 total, int threads) {
 template <typename T>
 int adrt_step_launch(const T *in, T *out, i64 batch, i64 n, int k, cudaStream_t st) {
   const i64 total = batch * 4 * (2 * n - 1) * n;
-  adrt_step_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(in, out, batch * 4, n, k);
+  const int lg = num_iters(n);
+  if (fits_u32(total))
+    adrt_step_kernel<T, unsigned><<<grid_for(total, 256), 256, 0, st>>>(in, out, (unsigned)total, (unsigned)n, lg, k);
+  else
+    adrt_step_kernel<T, unsigned long long><<<grid_for(total, 256), 256, 0, st>>>(
+        in, out, (unsigned long long)total, (unsigned long long)n, lg, k);
   return launch_status();
 }
 
@@ -77,7 +85,12 @@ template <typename T>
 int bdrt_step_launch(const T *in, T *out, i64 batch, i64 n, int k, cudaStream_t st) {
   const int L = num_iters(n);
   const i64 total = batch * 4 * (2 * n - 1) * n;
-  bdrt_step_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(in, out, batch * 4, n, L - k - 1);
+  if (fits_u32(total))
+    bdrt_step_kernel<T, unsigned><<<grid_for(total, 256), 256, 0, st>>>(in, out, (unsigned)total, (unsigned)n, L,
+                                                                        L - k - 1);
+  else
+    bdrt_step_kernel<T, unsigned long long><<<grid_for(total, 256), 256, 0, st>>>(
+        in, out, (unsigned long long)total, (unsigned long long)n, L, L - k - 1);
   return launch_status();
 }
 
