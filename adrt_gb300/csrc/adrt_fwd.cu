@@ -367,8 +367,10 @@ __device__ __forceinline__ void ragged_tile_S(int S, const FwdPassArgs &a, i64 t
 }
 
 // ctl[0]: next ticket, ctl[1]: error word.
+// Two CTAs per SM: the persistent loop inlines every stage count, and without
+// a bound the compiler spends registers that halve the resident CTAs.
 template <typename T>
-__global__ void __launch_bounds__(kFwdThreads)
+__global__ void __launch_bounds__(kFwdThreads, 2)
 ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__ inter,
                   const RaggedImage *__restrict__ imgs, const RaggedItem *__restrict__ items,
                   int n_items, unsigned *ctl, unsigned *counters, unsigned long long wait_ns) {

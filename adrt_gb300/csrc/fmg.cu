@@ -5,16 +5,19 @@ namespace adrtg {
 
 // out[p][r][c] = (x[p][2r][2c] + x[p][2r+1][2c]) / 4,  (4, 2n-1, n) -> (4, n-1, n/2).
 // Reference: src/adrt/adrt_cdefs_fmg.hpp:53-73.
-template <typename T>
+// Index arithmetic of these kernels runs in I: 32-bit unsigned when every
+// index fits (64-bit division is a long instruction sequence), else 64-bit.
+template <typename T, typename I>
 __global__ void fmg_restriction_kernel(const T *__restrict__ in, T *__restrict__ out,
-                                       i64 planes, i64 n) {
-  const i64 Ri = 2 * n - 1, Ro = n - 1, Co = n / 2;
-  const i64 total = planes * Ro * Co;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 c = idx % Co;
-    const i64 r = (idx / Co) % Ro;
-    const i64 p = idx / (Co * Ro);
+                                       I planes, I n) {
+  const I Ri = 2 * n - 1, Ro = n - 1, Co = n / 2;
+  const I total = planes * Ro * Co;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total;
+       idx += (I)gridDim.x * blockDim.x) {
+    const I c = idx % Co;
+    const I pr = idx / Co;
+    const I r = pr % Ro;
+    const I p = pr / Ro;
     const T va = in[(p * Ri + 2 * r) * n + 2 * c];
     const T vb = in[(p * Ri + 2 * r + 1) * n + 2 * c];
     out[idx] = div_rn(add_rn(va, vb), T(4));
@@ -23,15 +26,16 @@ __global__ void fmg_restriction_kernel(const T *__restrict__ in, T *__restrict__
 
 // 2x2 nearest-neighbour repeat, (h, w) -> (2h, 2w).
 // Reference: src/adrt/adrt_cdefs_fmg.hpp:75-95.
-template <typename T>
+template <typename T, typename I>
 __global__ void fmg_prolongation_kernel(const T *__restrict__ in, T *__restrict__ out,
-                                        i64 batch, i64 h, i64 w) {
-  const i64 total = batch * 4 * h * w;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 c = idx % (2 * w);
-    const i64 r = (idx / (2 * w)) % (2 * h);
-    const i64 b = idx / (4 * h * w);
+                                        I batch, I h, I w) {
+  const I total = batch * 4 * h * w;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total;
+       idx += (I)gridDim.x * blockDim.x) {
+    const I c = idx % (2 * w);
+    const I br = idx / (2 * w);
+    const I r = br % (2 * h);
+    const I b = br / (2 * h);
     out[idx] = in[(b * h + r / 2) * w + c / 2];
   }
 }
@@ -40,18 +44,19 @@ __global__ void fmg_prolongation_kernel(const T *__restrict__ in, T *__restrict_
 // reflected borders; taps multiplied then summed column by column:
 // (v11+v21+v31) + (v12+v22+v32) + (v13+v23+v33).
 // Reference: src/adrt/adrt_cdefs_fmg.hpp:97-171.
-template <typename T>
+template <typename T, typename I>
 __global__ void fmg_highpass_kernel(const T *__restrict__ in, T *__restrict__ out,
-                                    i64 batch, i64 h, i64 w) {
+                                    I batch, I h, I w) {
   const T ka = T(-0.0625), kb = T(-0.125), kc = T(0.75);
-  const i64 total = batch * h * w;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 c = idx % w;
-    const i64 r = (idx / w) % h;
-    const T *x = in + (idx / (h * w)) * h * w;
-    const i64 rp = r == 0 ? 1 : r - 1, rn = r == h - 1 ? r - 1 : r + 1;
-    const i64 cp = c == 0 ? 1 : c - 1, cn = c == w - 1 ? c - 1 : c + 1;
+  const I total = batch * h * w;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total;
+       idx += (I)gridDim.x * blockDim.x) {
+    const I c = idx % w;
+    const I br = idx / w;
+    const I r = br % h;
+    const T *x = in + (br / h) * h * w;
+    const I rp = r == 0 ? 1 : r - 1, rn = r == h - 1 ? r - 1 : r + 1;
+    const I cp = c == 0 ? 1 : c - 1, cn = c == w - 1 ? c - 1 : c + 1;
     const T v11 = mul_rn(ka, x[rp * w + cp]), v12 = mul_rn(kb, x[rp * w + c]),
             v13 = mul_rn(ka, x[rp * w + cn]);
     const T v21 = mul_rn(kb, x[r * w + cp]), v22 = mul_rn(kc, x[r * w + c]),
@@ -71,22 +76,42 @@ static unsigned grid_1d(i64 total) {
   return (unsigned)(g < 1 ? 1 : g);
 }
 
+// 32-bit indices when every index of the input and output, plus one grid
+// stride, stays below 2^32.
+static bool fits_u32(i64 max_index) { return max_index < (i64(1) << 32) - (i64(1) << 24); }
+
 template <typename T>
 int fmg_restriction_launch(const T *in, T *out, i64 batch, i64 n, cudaStream_t st) {
   const i64 total = batch * 4 * (n - 1) * (n / 2);
-  fmg_restriction_kernel<T><<<grid_1d(total), 256, 0, st>>>(in, out, batch * 4, n);
+  if (fits_u32(batch * 4 * (2 * n - 1) * n))
+    fmg_restriction_kernel<T, unsigned><<<grid_1d(total), 256, 0, st>>>(in, out, (unsigned)(batch * 4), (unsigned)n);
+  else
+    fmg_restriction_kernel<T, unsigned long long><<<grid_1d(total), 256, 0, st>>>(
+        in, out, (unsigned long long)(batch * 4), (unsigned long long)n);
   return launch_status();
 }
 
 template <typename T>
 int fmg_prolongation_launch(const T *in, T *out, i64 batch, i64 h, i64 w, cudaStream_t st) {
-  fmg_prolongation_kernel<T><<<grid_1d(batch * 4 * h * w), 256, 0, st>>>(in, out, batch, h, w);
+  const i64 total = batch * 4 * h * w;
+  if (fits_u32(total))
+    fmg_prolongation_kernel<T, unsigned><<<grid_1d(total), 256, 0, st>>>(in, out, (unsigned)batch, (unsigned)h,
+                                                                         (unsigned)w);
+  else
+    fmg_prolongation_kernel<T, unsigned long long><<<grid_1d(total), 256, 0, st>>>(
+        in, out, (unsigned long long)batch, (unsigned long long)h, (unsigned long long)w);
   return launch_status();
 }
 
 template <typename T>
 int fmg_highpass_launch(const T *in, T *out, i64 batch, i64 h, i64 w, cudaStream_t st) {
-  fmg_highpass_kernel<T><<<grid_1d(batch * h * w), 256, 0, st>>>(in, out, batch, h, w);
+  const i64 total = batch * h * w;
+  if (fits_u32(total))
+    fmg_highpass_kernel<T, unsigned><<<grid_1d(total), 256, 0, st>>>(in, out, (unsigned)batch, (unsigned)h,
+                                                                     (unsigned)w);
+  else
+    fmg_highpass_kernel<T, unsigned long long><<<grid_1d(total), 256, 0, st>>>(
+        in, out, (unsigned long long)batch, (unsigned long long)h, (unsigned long long)w);
   return launch_status();
 }
 

@@ -20,16 +20,20 @@ template <> struct word<16> { using t = w16; };
 // (n, n) image -> (4, 2n-1, n):  q0[c][a] = x[a][n-1-c], q1[c][a] = x[n-1-c][a],
 // q2[c][a] = x[c][a], q3[c][a] = x[n-1-a][n-1-c]; zero for c >= n.
 // Reference: src/adrt/core.py:170-175.
-template <typename W>
-__global__ void init_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n) {
-  const i64 C = 2 * n - 1;
-  const i64 total = batch * 4 * C * n;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 a = idx % n;
-    const i64 c = (idx / n) % C;
-    const int q = (int)((idx / (n * C)) % 4);
-    const i64 b = idx / (4 * n * C);
+// Index arithmetic of the copy kernels runs in I: 32-bit unsigned when every
+// index fits (64-bit division is a long instruction sequence), else 64-bit.
+template <typename W, typename I>
+__device__ __forceinline__ void init_body(const W *__restrict__ in, W *__restrict__ out, I batch, I n) {
+  const I C = 2 * n - 1;
+  const I total = batch * 4 * C * n;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total;
+       idx += (I)gridDim.x * blockDim.x) {
+    const I a = idx % n;
+    const I rq = idx / n;
+    const I c = rq % C;
+    const I bq = rq / C;
+    const int q = (int)(bq & 3);
+    const I b = bq >> 2;
     const W *x = in + b * n * n;
     W v = W(0);
     if (c < n) {
@@ -55,16 +59,17 @@ __device__ __forceinline__ i64 trunc_src(int q, i64 i, i64 j, i64 n) {
   }
 }
 
-template <typename W>
-__global__ void truncate_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n) {
-  const i64 C = 2 * n - 1;
-  const i64 total = batch * 4 * n * n;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 j = idx % n;
-    const i64 i = (idx / n) % n;
-    const i64 bq = idx / (n * n);
-    out[idx] = in[bq * C * n + trunc_src((int)(bq % 4), i, j, n)];
+template <typename W, typename I>
+__device__ __forceinline__ void truncate_body(const W *__restrict__ in, W *__restrict__ out, I batch, I n) {
+  const I C = 2 * n - 1;
+  const I total = batch * 4 * n * n;
+  for (I idx = blockIdx.x * (I)blockDim.x + threadIdx.x; idx < total;
+       idx += (I)gridDim.x * blockDim.x) {
+    const I j = idx % n;
+    const I r = idx / n;
+    const I i = r % n;
+    const I bq = r / n;
+    out[idx] = in[bq * C * n + (I)trunc_src((int)(bq & 3), i, j, n)];
   }
 }
 
@@ -138,6 +143,25 @@ __global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, I 
   }
 }
 
+template <typename W>
+__global__ void init_kernel_u32(const W *__restrict__ in, W *__restrict__ out, unsigned batch, unsigned n) {
+  init_body<W, unsigned>(in, out, batch, n);
+}
+template <typename W>
+__global__ void init_kernel_u64(const W *__restrict__ in, W *__restrict__ out, unsigned long long batch,
+                                unsigned long long n) {
+  init_body<W, unsigned long long>(in, out, batch, n);
+}
+template <typename W>
+__global__ void truncate_kernel_u32(const W *__restrict__ in, W *__restrict__ out, unsigned batch, unsigned n) {
+  truncate_body<W, unsigned>(in, out, batch, n);
+}
+template <typename W>
+__global__ void truncate_kernel_u64(const W *__restrict__ in, W *__restrict__ out, unsigned long long batch,
+                                    unsigned long long n) {
+  truncate_body<W, unsigned long long>(in, out, batch, n);
+}
+
 static unsigned grid_l(i64 total) {
   i64 g = (total + 255) / 256;
   if (g > 152 * 32) g = 152 * 32;
@@ -159,13 +183,27 @@ static unsigned grid_l(i64 total) {
     default: return ADRT_GB300_ERR_DTYPE;                                                   \
   }
 
+static bool fits_u32(i64 max_index) { return max_index < (i64(1) << 32) - (i64(1) << 24); }
+
 int init_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cudaStream_t st) {
-  BY_SIZE(es, init_kernel, batch * 4 * (2 * n - 1) * n, batch, n)
+  const i64 total = batch * 4 * (2 * n - 1) * n;
+  if (fits_u32(total)) {
+    const unsigned B = (unsigned)batch, N = (unsigned)n;
+    BY_SIZE(es, init_kernel_u32, total, B, N)
+  } else {
+    BY_SIZE(es, init_kernel_u64, total, (unsigned long long)batch, (unsigned long long)n)
+  }
   return launch_status();
 }
 
 int truncate_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cudaStream_t st) {
-  BY_SIZE(es, truncate_kernel, batch * 4 * n * n, batch, n)
+  const i64 total = batch * 4 * (2 * n - 1) * n;  // largest input index
+  if (fits_u32(total)) {
+    const unsigned B = (unsigned)batch, N = (unsigned)n;
+    BY_SIZE(es, truncate_kernel_u32, batch * 4 * n * n, B, N)
+  } else {
+    BY_SIZE(es, truncate_kernel_u64, batch * 4 * n * n, (unsigned long long)batch, (unsigned long long)n)
+  }
   return launch_status();
 }
 

@@ -118,6 +118,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
+def _host_mem_gb():
+    """(total, available) host memory in GB from /proc/meminfo, or None."""
+    try:
+        vals = {}
+        with open("/proc/meminfo") as f:
+            for line in f:
+                k, v = line.split(":", 1)
+                vals[k] = int(v.split()[0]) / 1e6
+        return [round(vals["MemTotal"], 1), round(vals["MemAvailable"], 1)]
+    except Exception:
+        return None
+
+
 def gpu_uuid(torch, dev) -> str:
     try:
         u = str(torch.cuda.get_device_properties(dev).uuid)
@@ -363,27 +376,35 @@ def main():
         # At least four calls (the first two allocate, the third still
         # settles), then until two in a row agree within 10 %.
         prev = None
+        warm_ms = []
         for i in range(10):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             yh = adrt.adrt(xh)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
+            warm_ms.append(round(dt * 1e3, 1))
             if i >= 3 and abs(dt - prev) <= 0.1 * prev:
                 break
             prev = dt
         barrier()
         torch.cuda.synchronize()
+        call_ms = []
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
+            tc = time.perf_counter()
             yh = adrt.adrt(xh)
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            call_ms.append(round((time.perf_counter() - tc) * 1e3, 1))
         t_e2e = max_over_ranks(time.perf_counter() - t0)
         e2e = {
             "value": world * B * args.e2e_steps / t_e2e,
             "unit": UNIT,
             "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
             "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
+            "warmup_call_ms": warm_ms,
+            "call_ms": call_ms,
+            "host_mem_gb": _host_mem_gb(),
         }
         del yh
 
