@@ -74,6 +74,13 @@ class _State:
     def stream(self):
         return torch.cuda.current_stream(self.dev).cuda_stream
 
+    def subset(self, sel: torch.Tensor) -> None:
+        """Keep only the images at positions `sel` (still-active ones)."""
+        for name in ("x", "r", "p", "rhs", "rs", "rhs2", "rs_new", "pAp", "active", "iters"):
+            setattr(self, name, getattr(self, name).index_select(0, sel).contiguous())
+        self.B = int(sel.numel())
+        self.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(self.B), dtype=torch.uint8, device=self.dev)
+
     def dot(self, a, b):
         out = torch.empty(self.B, dtype=torch.float64, device=self.dev)
         rc = _lib.load().adrt_gb300_batched_dot(a.data_ptr(), b.data_ptr(), out.data_ptr(), self.B,
@@ -102,9 +109,15 @@ class _State:
 
 
 def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, max_iters: int = 1000,
-       check_every: int = 4, graph: bool = False, ridge_param: float = 0.0) -> CGResult:
+       check_every: int = 4, graph: bool = False, ridge_param: float = 0.0, compact: float = 0.5) -> CGResult:
     """Batched CG for (A^T A + 4 ridge_param I) x = A^T b; b: CUDA tensor
-    (B, 4, 2n-1, n)."""
+    (B, 4, 2n-1, n).
+
+    Images converge after different numbers of iterations; when at most
+    `compact` of the images still iterating are active (checked every
+    `check_every` iterations), the finished ones are written out and the
+    batch shrinks to the active ones, so the work follows the iterations each
+    image needs rather than the slowest image's (0 disables)."""
     if not (isinstance(b, torch.Tensor) and b.is_cuda and b.ndim == 4):
         raise TypeError("cg expects a CUDA tensor of shape (B, 4, 2n-1, n)")
     if ridge_param < 0:
@@ -112,6 +125,12 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
     st = _State(b, x0, 4.0 * float(ridge_param))
     thr2 = st.rhs2 * (tol * tol)
     st.active.copy_((st.rs > thr2).to(torch.int32))
+    B_full = st.B
+    rhs_full, rhs2_full = st.rhs, st.rhs2
+    x_full = st.x
+    iters_full = torch.zeros(B_full, dtype=torch.int32, device=st.dev)
+    idx = torch.arange(B_full, device=st.dev)
+    compacted = False
     k = 0
     g = None
     while k < max_iters:
@@ -133,14 +152,35 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
             else:
                 st.iterate(thr2)
         k += steps
-        if not bool(st.active.any().item()):
+        n_active = int(st.active.sum().item())
+        if n_active == 0:
             break
+        if compact > 0 and st.B > 1 and n_active <= compact * st.B:
+            # Write every row back, then continue with the active images only
+            # (before the first shrink the state's tensors are the full ones).
+            if compacted:
+                x_full.index_copy_(0, idx, st.x)
+                iters_full.index_copy_(0, idx, st.iters)
+            else:
+                x_full, iters_full = st.x, st.iters
+            sel = st.active.nonzero().flatten()
+            idx = idx.index_select(0, sel)
+            st.subset(sel)
+            thr2 = thr2.index_select(0, sel).contiguous()
+            g = None
+            compacted = True
+    if compacted:
+        x_full.index_copy_(0, idx, st.x)
+        iters_full.index_copy_(0, idx, st.iters)
+    else:
+        iters_full = st.iters.clone()
     # Recompute the reported residuals from scratch.
-    res_n = normal_op(st.x, st.lam) - st.rhs
-    ax = _adrt(st.x)
+    st.B = B_full
+    st.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(B_full), dtype=torch.uint8, device=st.dev)
+    res_n = normal_op(x_full, st.lam) - rhs_full
+    ax = _adrt(x_full)
     dr = ax - b
-    normal_residual = torch.sqrt(st.dot(res_n, res_n) / st.rhs2)
-    B = st.B
-    nb = (b.reshape(B, -1).double() ** 2).sum(1)
-    data_residual = torch.sqrt((dr.reshape(B, -1).double() ** 2).sum(1) / nb)
-    return CGResult(st.x, st.iters.clone(), normal_residual, data_residual, k)
+    normal_residual = torch.sqrt(st.dot(res_n, res_n) / rhs2_full)
+    nb = (b.reshape(B_full, -1).double() ** 2).sum(1)
+    data_residual = torch.sqrt((dr.reshape(B_full, -1).double() ** 2).sum(1) / nb)
+    return CGResult(x_full, iters_full, normal_residual, data_residual, k)

@@ -352,7 +352,7 @@ class PreconditionerNet:
         _lib.check(self.lib.adrtnet_status(_stream(self.dev)), "adrtnet kernels")
 
     # ---- inference ------------------------------------------------------------
-    def predict(self, b: torch.Tensor, batch: int = 32) -> torch.Tensor:
+    def predict(self, b: torch.Tensor, batch: int = 256) -> torch.Tensor:
         """Starting images x0 (B, n, n) for data b (B, 4, 2n-1, n)."""
         bt = _adjoint(b.contiguous())
         out = torch.empty_like(bt)

@@ -174,7 +174,7 @@ def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
     }
 
 
-def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=30):
+def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=60):
     """Plain and learned-start batched CG on the normal equations of noisy
     256 x 256 ellipse phantoms (data b = adrt(x) + N(0, (1e-3 max|b|)^2)).
 

@@ -117,3 +117,20 @@ def test_ridge_matches_scipy_oracle(oracle_mod, ridge_param):
     # The ridge term shrinks the solution.
     assert (res.x.norm(dim=(1, 2)) < plain.x.norm(dim=(1, 2))).all()
     assert (res.normal_residual <= 1e-10).all()
+
+
+def test_compaction_gives_identical_results():
+    """Shrinking the batch to the active images changes no image's result."""
+    n, B = 64, 16
+    xt = ellipse_phantoms(B, n, seed=57, device="cuda")
+    b = adrt.adrt(xt)
+    # widely different difficulty: scale half of the batch's data
+    b[: B // 2] *= 1e-3
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    b = b + 1e-3 * b.abs().amax() * torch.randn(b.shape, generator=g, device="cuda")
+    full = cgmod.cg(b, tol=1e-5, max_iters=400, compact=0.0, check_every=1)
+    comp = cgmod.cg(b, tol=1e-5, max_iters=400, compact=0.9, check_every=1, graph=True)
+    assert torch.equal(full.iterations, comp.iterations)
+    assert torch.equal(full.x, comp.x)
+    assert torch.equal(full.normal_residual, comp.normal_residual)
