@@ -38,10 +38,12 @@ constexpr int NT = 256;           // threads per CTA
 constexpr int N = 1024;
 // After five stages a row group's values are non-zero only at offsets below
 // n + 31 (shifts reach 31); beyond that every value is +0, the sum of the
-// zero padding.  Pass A computes the tiles that hold those offsets and the
-// intermediate rows end there: pass B reads anything past the row end as +0.
+// zero padding.  The intermediate rows end there (rounded up to 8 floats) and
+// pass B reads anything past the row end as +0.  Pass A computes the tiles
+// that hold those offsets; in its last tile only the iterations and warps
+// that reach a stored offset run.
 constexpr int A_TILES = (N + 31 + W - 1) / W;  // 3
-constexpr int CS = A_TILES * W;                // 1440: intermediate row stride (32-byte multiple)
+constexpr int CS = (N + 31 + 7) / 8 * 8;       // 1056: intermediate row stride (128-byte multiple)
 constexpr unsigned FULL = 0xffffffffu;
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange buffer");
@@ -58,11 +60,6 @@ __device__ __forceinline__ void st8(float *p, const float (&v)[8]) {
                "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
                : "memory");
 }
-__device__ __forceinline__ void st8_stream(float *p, const float (&v)[8]) {
-  asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]),
-               "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
-               : "memory");
-}
 
 // Value of `cur` held by the lane D below (the previous chunk).  Lanes whose
 // previous chunk was handled in the previous iteration (lane < D) receive the
@@ -71,6 +68,17 @@ template <int D>
 __device__ __forceinline__ float prev_chunk(float cur, float saved, int lane) {
   const float send = (lane >= 32 - D) ? saved : cur;
   return __shfl_sync(FULL, send, (lane - D) & 31);
+}
+
+// Tile positions (from tbase) that group 1 must produce when the tile stores
+// `live` offsets from c0: group 2's block b reads positions up to 8b + 39,
+// the position of its own last output.
+__device__ __forceinline__ int needed_positions(int live) { return ((live + 7) & ~7) + HALO; }
+
+// Group-1 sweep iterations (128 positions each) covering `pos` positions.
+__device__ __forceinline__ int sweep_iters(int pos) {
+  const int it = (pos + 127) >> 7;
+  return it < NCH / 32 ? it : NCH / 32;
 }
 
 
@@ -203,13 +211,15 @@ __device__ __forceinline__ void put_exchange(float *xs, int mq, int ch, const fl
 
 // Pass A, quadrants 0 and 3: members are image rows, positions run along the
 // row from its right end (offset c <-> column n-1-c).  Warp = member quad.
-__device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase,
+__device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase, int pos,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
   constexpr int IT = NCH / 32;
+  const int nit = sweep_iters(pos);
   float4 raw[IT][4];
 #pragma unroll
   for (int it = 0; it < IT; ++it) {
+    if (it >= nit) break;
     const int ref0 = tbase + 4 * (it * 32 + lane);
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
@@ -223,6 +233,7 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
 #pragma unroll
   for (int it = 0; it < IT; ++it) {
+    if (it >= nit) break;
     float m[4][4];
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
@@ -239,10 +250,12 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
 // (q2) or up (q1) the columns.  A lane loads one 16-byte row segment (4
 // members) per position and transposes in registers.  Lanes: mq = lane & 7,
 // position group = lane >> 3; warp w sweeps chunks [16w - 1, 16w + 16), the
-// first one only to seed the boundary values.
-__device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r, int tbase,
+// first one only to seed the boundary values.  Warps whose chunks start at or
+// beyond `pos` have nothing to produce.
+__device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r, int tbase, int pos,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (64 * w >= pos) return;
   const int mq = lane & 7, pg = lane >> 3;
   constexpr int IT = 5;
   float4 raw[IT][4];
@@ -283,28 +296,41 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
 // selection of this lane's and the previous lane's 16-byte chunk.  Slot 0 of
 // `raw` holds the chunk that precedes the first one, seeding lane 0.
 template <int A4>
-__device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, float *xs,
+__device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, int pos, float *xs,
                                              size_t mstride, int cs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
   constexpr int IT = NCH / 32;
+  const int nit = sweep_iters(pos);
   float4 raw[IT + 1][4];
 #pragma unroll
   for (int jj = 0; jj < 4; ++jj) {
     const int j = 4 * mq + jj;
     const float *row = src + (size_t)j * mstride;
     const int gb = tbase - 4 * ((ap * j) >> 2);
+    if (gb >= 4 && gb + 128 * nit <= cs) {
+      // the whole sweep lies inside the row: no fill values (warp-uniform)
 #pragma unroll
-    for (int it = 0; it <= IT; ++it) {
-      // slot 0: the chunk before chunk 0 (only lane 31's copy is used)
-      const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
-      if (g0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
-      else if (g0 >= cs) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
-      else raw[it][jj] = ld4_stream(row + g0);
+      for (int it = 0; it <= IT; ++it) {
+        if (it > nit) break;
+        const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
+        raw[it][jj] = ld4_stream(row + g0);
+      }
+    } else {
+#pragma unroll
+      for (int it = 0; it <= IT; ++it) {
+        if (it > nit) break;
+        // slot 0: the chunk before chunk 0 (only lane 31's copy is used)
+        const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
+        if (g0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
+        else if (g0 >= cs) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else raw[it][jj] = ld4_stream(row + g0);
+      }
     }
   }
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
 #pragma unroll
   for (int it = 1; it <= IT; ++it) {
+    if (it > nit) break;
     float m[4][4];
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
@@ -417,8 +443,13 @@ __device__ __forceinline__ void group2_lane(int &b, bool &active, bool &store) {
   store = active && lane > 0;
 }
 
+// First stored block of this warp's half (lane 1): half 0 block 0, half 1
+// block 31.
+__device__ __forceinline__ int first_stored_block() { return (threadIdx.x >> 7) ? 31 : 0; }
+
 template <int L1>
 __device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, int c0) {
+  if (c0 + 8 * first_stored_block() >= CS) return;  // nothing this half stores
   int b;
   bool active, store;
   group2_lane(b, active, store);
@@ -441,13 +472,16 @@ __device__ __forceinline__ int ost_chunk(int row, int c) { return c ^ ((row >> 3
 
 template <int L1>
 __device__ __forceinline__ void group2_passB(const float *xs, float *ost, int c0, int n) {
+  // A half whose first stored offset is past the end stores nothing: the
+  // staged rows the store loop reads all come from the other half.
+  const bool idle = c0 + 8 * first_stored_block() >= 2 * n - 1;
   int b;
   bool active, store;
   group2_lane(b, active, store);
   float out[8][8];
-  group2_compute<L1, 0>(xs, b, active, out);
+  if (!idle) group2_compute<L1, 0>(xs, b, active, out);
   __syncthreads();  // every warp is done reading the exchange rows
-  if (!store) return;
+  if (!store || idle) return;
   // Rows 8b..8b+7 share the swizzle term b & 7: fixed offsets from one base.
   const int sw = b & 7;
   float *p0 = ost + 8 * b * 32 + 4 * ((2 * L1) ^ sw);
@@ -494,9 +528,10 @@ __global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__
   const int q = t % 4; t /= 4;
   const int bimg = t;
   const int c0 = ct * W, tbase = c0 - HALO;
+  const int pos = needed_positions(min(W, CS - c0));
   const float *img = in + (size_t)bimg * N * N;
-  if (q == 0 || q == 3) group1_passA_rows(img, q, r, tbase, xs);
-  else group1_passA_cols(img, q, r, tbase, xs);
+  if (q == 0 || q == 3) group1_passA_rows(img, q, r, tbase, pos, xs);
+  else group1_passA_cols(img, q, r, tbase, pos, xs);
   __syncthreads();
   float *dst_rows = inter + ((size_t)(bimg * 4 + q) * 32 + r) * 32 * CS;
   switch ((threadIdx.x >> 5) & 3) {
@@ -526,12 +561,13 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
   // member j row: inter[bimg][q][j][ap][*]
   const size_t mstride = (size_t)a_in * cs;
   const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * a_in + ap) * cs;
+  const int pos = needed_positions(min(W, 2 * n - 1 - c0));
   (void)err;
   switch (ap & 3) {
-    case 0: group1_passB<0>(src, ap, tbase, xs, mstride, cs); break;
-    case 1: group1_passB<1>(src, ap, tbase, xs, mstride, cs); break;
-    case 2: group1_passB<2>(src, ap, tbase, xs, mstride, cs); break;
-    default: group1_passB<3>(src, ap, tbase, xs, mstride, cs); break;
+    case 0: group1_passB<0>(src, ap, tbase, pos, xs, mstride, cs); break;
+    case 1: group1_passB<1>(src, ap, tbase, pos, xs, mstride, cs); break;
+    case 2: group1_passB<2>(src, ap, tbase, pos, xs, mstride, cs); break;
+    default: group1_passB<3>(src, ap, tbase, pos, xs, mstride, cs); break;
   }
   __syncthreads();
   float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
@@ -559,14 +595,20 @@ size_t fast_inter_bytes(i64 n) { return sizeof(float) * 4 * (size_t)n * fast_cs(
 
 bool fast_forward_eligible(i64 n, size_t elem) { return elem == 4 && n >= 64 && n <= fast::N; }
 
-// Images per chunk so that the chunk's intermediate stays in L2 (~48 MB;
-// 2 images at n = 1024), or the tuned budget.
+// Images per chunk (pass A then pass B per chunk).  Larger launches measured
+// faster than chunks whose intermediate stays in L2 (n = 1024, 256 images:
+// 52.1k img/s with one launch pair, 46.9k with 5-image chunks): the launch
+// tails cost more than the intermediate's round trip through HBM, which has
+// bandwidth to spare here.  Built-in budget 4 GB of intermediate (236 images
+// at n = 1024), or the tuned one; chunks are balanced so the last one is not
+// a small tail.
 static i64 fast_chunk(i64 batch, i64 n) {
   const int mb = tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).chunk_mb;
-  i64 k = (i64)(((size_t)(mb > 0 ? mb : 48) << 20) / fast_inter_bytes(n));
+  i64 k = (i64)(((size_t)(mb > 0 ? mb : 4096) << 20) / fast_inter_bytes(n));
   if (k < 1) k = 1;
-  if (n == fast::N && mb == 0) k = 2;
-  return batch < k ? batch : k;
+  if (batch <= k) return batch;
+  const i64 nchunks = (batch + k - 1) / k;
+  return (batch + nchunks - 1) / nchunks;
 }
 
 size_t fast_workspace_bytes(i64 batch, i64 n) { return fast_inter_bytes(n) * (size_t)fast_chunk(batch, n); }

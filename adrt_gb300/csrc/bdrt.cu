@@ -212,13 +212,19 @@ static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cuda
   return bwd_dispatch_S<T, false, false>(S, a, st);
 }
 
+// Images per chunk.  One chunk's intermediate has a built-in budget of 1 GB
+// (bdrt at n = 1024, float32, 128 images: 9.9k img/s against 8.5k with
+// 48 MB chunks whose intermediate stays in L2: fewer launch tails), or the
+// tuned one; chunks are balanced.
 static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
   const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
   const int mb = tune_lookup(ADRT_GB300_OP_BDRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).chunk_mb;
-  const size_t budget = (size_t)(mb > 0 ? mb : 48) << 20;
+  const size_t budget = (size_t)(mb > 0 ? mb : 1024) << 20;
   i64 k = (i64)(budget / per);
   if (k < 1) k = 1;
-  return k < batch ? k : batch;
+  if (batch <= k) return batch;
+  const i64 nchunks = (batch + k - 1) / k;
+  return (batch + nchunks - 1) / nchunks;
 }
 
 size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {

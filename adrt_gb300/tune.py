@@ -10,7 +10,8 @@ never the arithmetic), and installs the fastest in the library's table
 * ``width``: forward tile width in offsets, 128 or 256;
 * ``max_fused``: stages fused in shared memory per pass (3, 4 or 5), which
   sets the number of passes through HBM/L2;
-* ``chunk_mb``: L2 budget of one chunk's intermediate buffer;
+* ``chunk_mb``: budget of one chunk's intermediate buffer (images per
+  launch: small chunks keep it in L2, large ones cut launch tails);
 * ``use_fast``: the float32 fast forward kernels (64 <= n <= 1024) or the
   generic pass kernels.
 
@@ -83,7 +84,7 @@ def candidates(op: str, n: int, dtype) -> list:
     """Configurations worth timing for (op, n, dtype); the built-in one first."""
     L = max(0, n.bit_length() - 1)
     fused = [0] + [m for m in (4, 3) if m < L and -(-L // m) != -(-L // 5)]
-    chunks = [0, 24, 72, 96]
+    chunks = [0, 96, 1024]
     out = [Config()]
     if op == "adrt":
         fast = [-1, 0] if (_dt(dtype) == _lib.F32 and 64 <= n <= 1024) else [-1]

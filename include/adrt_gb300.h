@@ -69,8 +69,9 @@ uint64_t adrt_gb300_launch_count(void);
  * path).  Per (op in {ADRT_GB300_OP_ADRT, ADRT_GB300_OP_BDRT}, dtype, n a
  * power of two): width = forward tile width in offsets (0, 128 or 256),
  * max_fused = stages fused in shared memory per pass (0 = built-in 5, or
- * 1..5), chunk_mb = L2 budget of one chunk's intermediate in MB (0 =
- * built-in), use_fast = float32 fast forward kernels (-1 = when eligible,
+ * 1..5), chunk_mb = budget of one chunk's intermediate in MB, i.e. images
+ * per launch (0 = built-in: 4096 for the float32 fast forward, 1024 for bdrt, 48
+ * otherwise), use_fast = float32 fast forward kernels (-1 = when eligible,
  * 0 = off, 1 = on when eligible).  Results are bit-identical for every
  * setting; only speed changes.  Not synchronised with calls in flight on
  * other threads: set the table before launching work.  Workspace sizes

@@ -93,9 +93,9 @@ def test_workspace_sizes(lib):
     # One pass (n <= 32) needs no intermediate.
     assert _lib.workspace_size(_lib.OP_ADRT, 4, 32, _lib.F32) == 0
     # Two passes: one intermediate per image in the chunk; at n = 1024 the
-    # fast float32 path keeps the 1440 offsets (3 tiles of 480) where a row
+    # fast float32 path keeps the 1056 offsets (n + 31 rounded up to 8) where a row
     # group can be non-zero after five stages.
-    per = 4 * 32 * 32 * 1440 * 4
+    per = 4 * 32 * 32 * 1056 * 4
     got = _lib.workspace_size(_lib.OP_ADRT, 256, 1024, _lib.F32)
     assert got > 0 and got % per == 0
     per64 = 4 * 512 * 1023 * 8
