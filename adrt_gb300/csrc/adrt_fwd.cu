@@ -41,6 +41,10 @@ static int fwd_width(long long n, int dtype) {
 template <typename T> constexpr int dtype_code() { return sizeof(T) == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64; }
 constexpr int kFwdHalo = 32;  // halo columns kept left of the tile (>= 2^S - 1)
 constexpr int kFwdThreads = 256;
+// Threads per CTA of the pass kernels (the ragged kernel uses kFwdThreads):
+// 512 for float64 passes of five stages (measured 1.15x faster at n = 1024),
+// 256 otherwise (float32 five-stage passes measured 3 % slower with 512).
+template <typename T, int S> constexpr int fwd_threads() { return (sizeof(T) == 8 && S >= 5) ? 512 : 256; }
 
 struct FwdPassArgs {
   const void *in;  // image (first pass) or stage-k0 buffer
@@ -58,15 +62,15 @@ struct FwdPassArgs {
 // consecutive rows: the row stride is TWP (a multiple of 32) plus PAD, chosen
 // so that the rows and positions one shared-memory wavefront covers (32 lanes
 // of 4-byte, 16 of 8-byte elements) fall in distinct banks.
-template <typename T, int ROWS, int W>
+template <typename T, int ROWS, int W, int NT = kFwdThreads>
 struct FwdTile {
   static constexpr int TWP = W + kFwdHalo;                  // positions per row
   static constexpr int WF = sizeof(T) == 4 ? 32 : 16;       // lanes per wavefront
   static constexpr int PAD = ROWS == 1 ? 0 : (ROWS >= WF ? 1 : WF / ROWS);
   static constexpr int RS = TWP + PAD;
   static constexpr int BUF = ROWS * RS;
-  static constexpr int TPR = ROWS >= 8 ? 32 : kFwdThreads / ROWS;  // threads per row
-  static constexpr int ROW_STEP = kFwdThreads / TPR;               // rows in flight
+  static constexpr int TPR = ROWS >= 8 ? 32 : NT / ROWS;  // threads per row
+  static constexpr int ROW_STEP = NT / TPR;               // rows in flight
   static_assert(TWP % 32 == 0, "tile width plus halo must be a multiple of 32");
 };
 
@@ -77,11 +81,11 @@ __device__ __forceinline__ T ld_l2(const T *p) { return __ldcg(p); }
 
 // One tile of one pass.  `tile` enumerates (b, q, r, a', column tile), column
 // tile fastest; `smem_raw` holds two tile buffers.
-template <typename T, int S, bool FIRST, bool LAST, int kFwdW>
+template <typename T, int S, bool FIRST, bool LAST, int kFwdW, int NT = kFwdThreads>
 __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
                                          unsigned char *smem_raw) {
   constexpr int ROWS = 1 << S;
-  using TL = FwdTile<T, ROWS, kFwdW>;
+  using TL = FwdTile<T, ROWS, kFwdW, NT>;
   constexpr int TWP = TL::TWP, RS = TL::RS;
   T *buf0 = reinterpret_cast<T *>(smem_raw);
   T *buf1 = buf0 + TL::BUF;
@@ -111,35 +115,40 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   // Offsets below 0 do not exist in the reference (it copies instead of adding
   // there); they are stored as -0.0, and e + (-0) == e for every e, so the
   // stages below add unconditionally.  Offsets n..2n-2 of the first pass are
-  // the reference's +0 padding.
+  // the reference's +0 padding.  Offsets inside one image or quadrant are
+  // 32-bit (n <= 32768, checked by the host).
+  const unsigned un = (unsigned)n;
   if (FIRST) {
-    const T *img = static_cast<const T *>(args.in) + b * n * n;
+    const T *img = static_cast<const T *>(args.in) + (size_t)b * un * un;
     const bool col_major = (q == 1 || q == 2);
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
       int i, u;
       if (col_major) { i = idx % ROWS; u = idx / ROWS; }
       else { i = idx / TWP; u = idx % TWP; }
-      const i64 ref = tbase + u;  // a' == 0 in the first pass
-      const i64 R0 = r * ROWS + i;
+      const int ref = (int)tbase + u;  // a' == 0 in the first pass
+      const unsigned R0 = (unsigned)r * ROWS + i;
       T v = ref < 0 ? T(-0.0) : T(0);
-      if (ref >= 0 && ref < n) {
+      if (ref >= 0 && ref < (int)un) {
+        const unsigned c = (unsigned)ref;
         switch (q) {
-          case 0: v = img[R0 * n + (n - 1 - ref)]; break;
-          case 1: v = img[(n - 1 - ref) * n + R0]; break;
-          case 2: v = img[ref * n + R0]; break;
-          default: v = img[(n - 1 - R0) * n + (n - 1 - ref)]; break;
+          case 0: v = img[R0 * un + (un - 1 - c)]; break;
+          case 1: v = img[(un - 1 - c) * un + R0]; break;
+          case 2: v = img[c * un + R0]; break;
+          default: v = img[(un - 1 - R0) * un + (un - 1 - c)]; break;
         }
       }
       buf0[i * RS + u] = v;
     }
   } else {
-    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * R_in * A_in * C;
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+    const T *src = static_cast<const T *>(args.in) + ((size_t)b * 4 + q) * un * (size_t)C;
+    const unsigned row0 = (unsigned)r * ROWS * (unsigned)A_in + (unsigned)ap;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
       const int i = idx / TWP, u = idx % TWP;
-      const i64 ref = tbase + u - ap * i;
-      const i64 row = (r * ROWS + i) * A_in + ap;
+      const int ref = (int)tbase + u - (int)ap * i;
       T v = ref < 0 ? T(-0.0) : T(0);
-      if (ref >= 0 && ref < C) v = ld_l2(&src[row * C + ref]);
+      if (ref >= 0 && ref < (int)C) v = ld_l2(&src[(row0 + (unsigned)i * (unsigned)A_in) * (unsigned)C + (unsigned)ref]);
       buf0[i * RS + u] = v;
     }
   }
@@ -167,28 +176,30 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   // ---- store: local angle l is global angle a' * 2^S + l of row group r.
   if (LAST) {
     // out[b][q][c][a], angle innermost; here R_out == 1 and A_out == n.
-    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * C * n;
-    for (int idx = threadIdx.x; idx < kFwdW * ROWS; idx += blockDim.x) {
+    T *dst = static_cast<T *>(args.out) + ((size_t)b * 4 + q) * (size_t)C * un + (unsigned)ap * ROWS;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < kFwdW * ROWS; idx += NT) {
       const int l = idx % ROWS, w = idx / ROWS;
-      const i64 c = c0 + w;
-      if (c < C) st_stream(&dst[c * n + ap * ROWS + l], cur[l * RS + kFwdHalo + w]);
+      const int c = (int)c0 + w;
+      if (c < (int)C) st_stream(&dst[(unsigned)c * un + l], cur[l * RS + kFwdHalo + w]);
     }
   } else {
-    const i64 cs = args.cs_out ? args.cs_out : C;
-    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * R_out * A_out * cs;
-    for (int idx = threadIdx.x; idx < ROWS * kFwdW; idx += blockDim.x) {
+    const unsigned cs = args.cs_out ? (unsigned)args.cs_out : (unsigned)C;
+    T *dst = static_cast<T *>(args.out) + ((size_t)b * 4 + q) * un * (size_t)cs +
+             ((size_t)r * A_out + (size_t)ap * ROWS) * cs + c0;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * kFwdW; idx += NT) {
       const int l = idx / kFwdW, w = idx % kFwdW;
-      const i64 c = c0 + w;
-      if (c < C) dst[(r * A_out + ap * ROWS + l) * cs + c] = cur[l * RS + kFwdHalo + w];
+      if ((int)c0 + w < (int)C) dst[(unsigned)l * cs + (unsigned)w] = cur[l * RS + kFwdHalo + w];
     }
   }
 }
 
 template <typename T, int S, bool FIRST, bool LAST, int W>
-__global__ void __launch_bounds__(kFwdThreads)
+__global__ void __launch_bounds__(fwd_threads<T, S>())
 fwd_pass_kernel(FwdPassArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  fwd_tile<T, S, FIRST, LAST, W>(args, blockIdx.x, smem_raw);
+  fwd_tile<T, S, FIRST, LAST, W, fwd_threads<T, S>()>(args, blockIdx.x, smem_raw);
 }
 
 // Tiles in one pass of one image for tile width W.
@@ -214,7 +225,7 @@ static int launch_fwd_pass_w(const FwdPassArgs &a, cudaStream_t st) {
     configured = true;
   }
   const i64 tiles = a.batch * fwd_pass_tiles(a.n, S, W);
-  kern<<<(unsigned)tiles, kFwdThreads, smem, st>>>(a);
+  kern<<<(unsigned)tiles, fwd_threads<T, S>(), smem, st>>>(a);
   return launch_status();
 }
 
@@ -293,6 +304,8 @@ int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
       return adrt_forward_fast(reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out),
                                batch, n, ws, ws_bytes, st);
   }
+  // The pass kernels index one image or quadrant (n (2n-1) elements) in 32 bits.
+  if (n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
   int sizes[16];
   const int P = plan_passes(num_iters(n), sizes, fwd_max_fused(n, sizeof(T)));
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);

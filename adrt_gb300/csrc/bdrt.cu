@@ -23,9 +23,14 @@
 
 namespace adrtg {
 
-constexpr int kBwdW = 128;
+// Tile width in stored offsets: 224 for float32 (tile rows of 256 positions
+// with the halo, three CTAs per SM), 128 for float64 (two CTAs per SM).
+template <typename T> constexpr int bwd_width() { return sizeof(T) == 4 ? 224 : 128; }
 constexpr int kBwdHalo = 32;   // right halo (>= 2^S - 1)
-constexpr int kBwdThreads = 256;
+// Threads per CTA: 512 for passes of five stages (32 tile rows; measured
+// 1.4x faster than 256 at n = 1024), 256 for shorter passes (slightly faster
+// there).  Occupancy is bound by shared memory, three CTAs per SM.
+template <int S> constexpr int bwd_threads() { return S >= 5 ? 512 : 256; }
 
 struct BwdPassArgs {
   const void *in;  // final-layout array (first pass) or bdrt buffer
@@ -44,69 +49,78 @@ struct BwdPassArgs {
 // padded so the transposing first-pass loads and last-pass stores hit
 // distinct banks.  A 32-element tail pad keeps the right-shifted reads of the
 // last row in bounds.
-template <typename T, int ROWS>
+template <typename T, int ROWS, int NT>
 struct BwdTile {
-  static constexpr int TWP = kBwdW + kBwdHalo;
+  static constexpr int W = bwd_width<T>();
+  static constexpr int TWP = W + kBwdHalo;
   static constexpr int WF = sizeof(T) == 4 ? 32 : 16;  // lanes per wavefront
   static constexpr int PAD = ROWS == 1 ? 0 : (ROWS >= WF ? 1 : WF / ROWS);
   static constexpr int RS = TWP + PAD;
   static constexpr int BUF = ROWS * RS + 32;
-  static constexpr int TPR = ROWS >= 8 ? 32 : kBwdThreads / ROWS;
-  static constexpr int ROW_STEP = kBwdThreads / TPR;
+  static constexpr int TPR = ROWS >= 8 ? 32 : NT / ROWS;
+  static constexpr int ROW_STEP = NT / TPR;
   static_assert(TWP % 32 == 0, "tile width plus halo must be a multiple of 32");
 };
 
+// Column tiles of one pass: tile positions span [0, C + a'_max * (2^S - 1)) so
+// every member's pre-shifted window is covered.
+static __host__ __device__ inline int bwd_col_tiles(i64 n, int k0, int S, int W) {
+  const i64 C = 2 * n - 1;
+  const i64 max_ext = ((i64(1) << k0) - 1) * ((1 << S) - 1);
+  return (int)((C + max_ext + W - 1) / W);
+}
+
+// Per-quadrant index arithmetic is 32-bit: a quadrant holds n (2n-1) < 2^32
+// elements for every n the host accepts here (checked in bdrt_forward).
 template <typename T, int S, bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kBwdThreads)
+__global__ void __launch_bounds__(bwd_threads<S>())
 bwd_pass_kernel(BwdPassArgs args) {
-  constexpr int ROWS = 1 << S;
-  using TL = BwdTile<T, ROWS>;
-  constexpr int TWP = TL::TWP, RS = TL::RS;
+  constexpr int ROWS = 1 << S, NT = bwd_threads<S>();
+  using TL = BwdTile<T, ROWS, NT>;
+  constexpr int W = TL::W, TWP = TL::TWP, RS = TL::RS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf0 = reinterpret_cast<T *>(smem_raw);
   T *buf1 = buf0 + TL::BUF;
 
-  const i64 n = args.n;
-  const i64 C = 2 * n - 1;
+  const unsigned n = (unsigned)args.n;
+  const int C = (int)(2 * args.n - 1);
   const int k0 = args.k0;
-  const i64 A_lo = i64(1) << k0;   // angles after this pass (pass output)
-  const i64 R_lo = n >> k0;        // sections after this pass
-  const i64 A_hi = A_lo << S;      // angles at pass input
-  const i64 R_hi = R_lo >> S;      // sections at pass input
-  // Tile positions span [0, C + a'*(2^S-1)) so every member's window is covered.
-  const i64 max_ext = (A_lo - 1) * (ROWS - 1);
-  const int col_tiles = (int)((C + max_ext + kBwdW - 1) / kBwdW);
+  const unsigned A_lo = 1u << k0;      // angles after this pass (pass output)
+  const unsigned R_lo = n >> k0;       // sections after this pass
+  const unsigned R_hi = R_lo >> S;     // sections at pass input
+  const int col_tiles = bwd_col_tiles(args.n, k0, S, W);
 
-  // 32-bit decode (64-bit division is a long instruction sequence).
   unsigned t = blockIdx.x;
   const int ct = (int)(t % (unsigned)col_tiles); t /= (unsigned)col_tiles;
-  const i64 ap = t % (unsigned)A_lo; t /= (unsigned)A_lo;
-  const i64 r = t % (unsigned)R_hi; t /= (unsigned)R_hi;
-  const int q = (int)(t & 3u); t >>= 2;
-  const i64 b = t;
-  const i64 c0 = (i64)ct * kBwdW;
+  const unsigned ap = t % A_lo; t /= A_lo;
+  const unsigned r = t % R_hi; t /= R_hi;
+  const unsigned q = t & 3u; t >>= 2;
+  const unsigned b = t;
+  const int c0 = ct * W;
   // Skip tiles that hold no member's needed offsets (member i of this tile
   // stores reference offsets >= c0 - a'*i).
-  if (c0 >= args.c_need + ap * (ROWS - 1)) return;
+  if ((i64)c0 >= args.c_need + (i64)ap * (ROWS - 1)) return;
+  const size_t qoff = ((size_t)b * 4 + q) * (size_t)n * (size_t)C;  // quadrant base
 
   // ---- load angle l = a'*2^S + l of section r, tile positions [c0, c0+TWP).
   if (FIRST) {
     // in[b][q][c][angle], angle innermost; here R_hi == 1, A_hi == n.
-    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * C * n;
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+    const T *src = static_cast<const T *>(args.in) + qoff + ap * ROWS;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
       const int l = idx % ROWS, u = idx / ROWS;
-      const i64 c = c0 + u;
+      const int c = c0 + u;
       T v = T(0);
-      if (c < C) v = src[c * n + ap * ROWS + l];
+      if (c < C) v = src[(unsigned)c * n + l];
       buf0[l * RS + u] = v;
     }
   } else {
-    const T *src = static_cast<const T *>(args.in) + (b * 4 + q) * A_hi * R_hi * C;
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += blockDim.x) {
+    const T *src = static_cast<const T *>(args.in) + qoff + ((size_t)ap * ROWS * R_hi + r) * C + c0;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
       const int l = idx / TWP, u = idx % TWP;
-      const i64 c = c0 + u;
       T v = T(0);
-      if (c < C) v = src[((ap * ROWS + l) * R_hi + r) * C + c];
+      if (c0 + u < C) v = src[(unsigned)l * R_hi * (unsigned)C + u];
       buf0[l * RS + u] = v;
     }
   }
@@ -115,6 +129,9 @@ bwd_pass_kernel(BwdPassArgs args) {
   // ---- S transposed stages, forward local stage j = S-1 down to 0.
   // Level j+1 buffer rows: combo m, local angle la -> row m * 2^(j+1) + la.
   // Level j buffer rows:   combo m', local angle li -> row m' * 2^j + li.
+  // Right rows: tile position u holds reference offset base + u of la; the
+  // reference adds la + lbb while that offset is <= C - 2, copies la at C - 1
+  // and writes +0 beyond.  The three ranges are computed once per row.
   T *cur = buf0, *nxt = buf1;
   const int lr = threadIdx.x % TL::TPR;
 #pragma unroll
@@ -129,17 +146,21 @@ bwd_pass_kernel(BwdPassArgs args) {
       T *np = nxt + rowo * RS;
       if ((mm & 1) == 0) {
         // left: la + lb (positions past the buffer end are never used)
+#pragma unroll
         for (int u = lr; u < TWP; u += TL::TPR) np[u] = add_rn(ya[u], yb[u]);
       } else {
         // right: reference offset of la is base + u, with the parent mapping a'*2m*2^j.
-        const i64 base = c0 + li - ap * (i64)((2 * m) << j);
-        const i64 last_add = C - 2 - base;  // u <= last_add: la + lbb
-        for (int u = lr; u < TWP; u += TL::TPR) {
-          T v;
-          if (u <= last_add) v = add_rn(ya[u + li], yb[u + li + 1]);
-          else if (u == last_add + 1) v = ya[u + li];  // copy of la at offset C-1
-          else v = T(0);
-          np[u] = v;
+        const int base = c0 + li - (int)(ap * (unsigned)((2 * m) << j));
+        const int copy_at = C - 1 - base;  // la + lbb below, copy of la here, +0 beyond
+        ya += li;
+        yb += li + 1;
+        if (copy_at >= TWP) {
+#pragma unroll
+          for (int u = lr; u < TWP; u += TL::TPR) np[u] = add_rn(ya[u], yb[u]);
+        } else {
+#pragma unroll
+          for (int u = lr; u < TWP; u += TL::TPR)
+            np[u] = u < copy_at ? add_rn(ya[u], yb[u]) : (u == copy_at ? ya[u] : T(0));
         }
       }
     }
@@ -150,18 +171,20 @@ bwd_pass_kernel(BwdPassArgs args) {
   // ---- store member i (section r*2^S + i at angle a') at reference offset u + c0 - a'*i.
   if (LAST) {
     // out[b][q][c][section], section innermost; A_lo == 1, a' == 0.
-    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * C * n;
-    for (int idx = threadIdx.x; idx < kBwdW * ROWS; idx += blockDim.x) {
+    T *dst = static_cast<T *>(args.out) + qoff + r * ROWS;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < W * ROWS; idx += NT) {
       const int i = idx % ROWS, w = idx / ROWS;
-      const i64 c = c0 + w;
-      if (c < C) st_stream(&dst[c * n + r * ROWS + i], cur[i * RS + w]);
+      const int c = c0 + w;
+      if (c < C) st_stream(&dst[(unsigned)c * n + i], cur[i * RS + w]);
     }
   } else {
-    T *dst = static_cast<T *>(args.out) + (b * 4 + q) * A_lo * R_lo * C;
-    for (int idx = threadIdx.x; idx < ROWS * kBwdW; idx += blockDim.x) {
-      const int i = idx / kBwdW, w = idx % kBwdW;
-      const i64 c = c0 + w - ap * i;
-      if (c >= 0 && c < C) dst[(ap * R_lo + r * ROWS + i) * C + c] = cur[i * RS + w];
+    T *dst = static_cast<T *>(args.out) + qoff + ((size_t)ap * R_lo + r * ROWS) * C;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ROWS * W; idx += NT) {
+      const int i = idx / W, w = idx % W;
+      const int c = c0 + w - (int)ap * i;
+      if (c >= 0 && c < C) dst[(unsigned)i * (unsigned)C + (unsigned)c] = cur[i * RS + w];
     }
   }
 }
@@ -174,20 +197,18 @@ static int plan_passes_bwd(i64 n, size_t elem, int *sizes) {
 
 template <typename T, int S, bool FIRST, bool LAST>
 static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
-  constexpr int ROWS = 1 << S;
-  const size_t smem = 2 * sizeof(T) * BwdTile<T, ROWS>::BUF;
+  constexpr int ROWS = 1 << S, NT = bwd_threads<S>();
+  const size_t smem = 2 * sizeof(T) * BwdTile<T, ROWS, NT>::BUF;
   auto kern = bwd_pass_kernel<T, S, FIRST, LAST>;
   static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
-  const i64 C = 2 * a.n - 1;
   const i64 A_lo = i64(1) << a.k0;
-  const i64 max_ext = (A_lo - 1) * (ROWS - 1);
-  const i64 col_tiles = (C + max_ext + kBwdW - 1) / kBwdW;
+  const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W);
   const i64 tiles = a.batch * 4 * ((a.n >> a.k0) >> S) * A_lo * col_tiles;
-  kern<<<(unsigned)tiles, kBwdThreads, smem, st>>>(a);
+  kern<<<(unsigned)tiles, NT, smem, st>>>(a);
   return launch_status();
 }
 
@@ -243,6 +264,8 @@ size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
 template <typename T>
 int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st, i64 rows_needed) {
+  // The pass kernels index one quadrant (n (2n-1) elements) in 32 bits.
+  if (n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
   int sizes[16];
   const int P = plan_passes_bwd(n, sizeof(T), sizes);
   const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
