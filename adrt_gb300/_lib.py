@@ -78,6 +78,7 @@ SIGNATURES = {
     "adrt_gb300_cg_update": [_v, _v, _v, _v, _v, _v, _v, _v, _i64, _i64, _int, _v, _v],
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
     "adrt_gb300_axpy": [ctypes.c_double, _v, _v, _i64, _int, _v],
+    "adrt_gb300_precond_conv": [_v, _v, _i64, _i64, ctypes.POINTER(ctypes.c_double), _int, _int, _v],
     "adrt_gb300_tune_set": [_int, _int, _i64, _int, _int, _int, _int],
     "adrt_gb300_tune_get": [_int, _int, _i64, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int),
                             ctypes.POINTER(_int)],

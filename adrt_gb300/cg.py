@@ -16,6 +16,12 @@ Each image stops when its normal-equation residual
 batch runs until all images stopped or `max_iters`.  All vector algebra runs
 in the library's CG kernels with float64 per-image scalars; with
 ``graph=True`` one CG iteration is captured in a CUDA graph and replayed.
+
+With ``precond`` (a symmetric positive definite operator with an
+``apply(x, out)`` method, e.g. ``adrt_gb300.precond.ConvPreconditioner``)
+the iteration is preconditioned CG: z = M r, alpha = <r, z> / <p, A^T A p>,
+p = z + beta p with beta = <r_new, z_new> / <r, z>; the stopping rule stays
+the unpreconditioned normal-equation residual above.
 """
 
 from __future__ import annotations
@@ -29,7 +35,7 @@ from ._ops import adrt as _adrt
 from .autograd import _adjoint_raw as _adjoint
 from ._wrappers import float_code
 
-__all__ = ["normal_op", "cg", "CGResult"]
+__all__ = ["normal_op", "cg", "residuals_of", "CGResult"]
 
 
 def normal_op(x: torch.Tensor, lam: float = 0.0) -> torch.Tensor:
@@ -52,8 +58,9 @@ class CGResult:
 
 
 class _State:
-    def __init__(self, b, x0, lam=0.0):
+    def __init__(self, b, x0, lam=0.0, precond=None):
         self.lam = lam
+        self.precond = precond
         self.dev = b.device
         self.B = b.shape[0]
         n = b.shape[-1]
@@ -62,9 +69,18 @@ class _State:
         self.x = torch.zeros((self.B, n, n), dtype=b.dtype, device=b.device) if x0 is None else x0.clone().contiguous()
         self.rhs = _adjoint(b.contiguous())
         self.r = self.rhs - normal_op(self.x, lam) if x0 is not None else self.rhs.clone()
-        self.p = self.r.clone()
         self.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(self.B), dtype=torch.uint8, device=b.device)
-        self.rs = self.dot(self.r, self.r)
+        # rs: numerator of alpha (<r, r>, or <r, z> when preconditioned);
+        # rr: <r, r> for the stopping rule.
+        self.rr = self.dot(self.r, self.r)
+        if precond is not None:
+            self.z = precond.apply(self.r)
+            self.p = self.z.clone()
+            self.rs = self.dot(self.r, self.z)
+            self.rz_new = torch.empty_like(self.rs)
+        else:
+            self.p = self.r.clone()
+            self.rs = self.rr.clone()
         self.rhs2 = self.dot(self.rhs, self.rhs)
         self.rs_new = torch.empty_like(self.rs)
         self.pAp = torch.empty_like(self.rs)
@@ -76,7 +92,10 @@ class _State:
 
     def subset(self, sel: torch.Tensor) -> None:
         """Keep only the images at positions `sel` (still-active ones)."""
-        for name in ("x", "r", "p", "rhs", "rs", "rhs2", "rs_new", "pAp", "active", "iters"):
+        names = ["x", "r", "p", "rhs", "rs", "rr", "rhs2", "rs_new", "pAp", "active", "iters"]
+        if self.precond is not None:
+            names += ["z", "rz_new"]
+        for name in names:
             setattr(self, name, getattr(self, name).index_select(0, sel).contiguous())
         self.B = int(sel.numel())
         self.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(self.B), dtype=torch.uint8, device=self.dev)
@@ -102,14 +121,23 @@ class _State:
         _lib.check(rc, "cg_update")
         # Images whose residual reached the tolerance stop here.
         self.active.mul_((self.rs_new > thr2).to(torch.int32))
-        rc = lib.adrt_gb300_cg_direction(self.p.data_ptr(), self.r.data_ptr(), self.rs_new.data_ptr(),
+        if self.precond is not None:
+            self.precond.apply(self.r, out=self.z)
+            rc = lib.adrt_gb300_batched_dot(self.r.data_ptr(), self.z.data_ptr(), self.rz_new.data_ptr(), self.B,
+                                            self.per, self.code, self.ws.data_ptr(), self.stream())
+            _lib.check(rc, "batched_dot")
+            d, num = self.z, self.rz_new
+        else:
+            d, num = self.r, self.rs_new
+        rc = lib.adrt_gb300_cg_direction(self.p.data_ptr(), d.data_ptr(), num.data_ptr(),
                                          self.rs.data_ptr(), self.active.data_ptr(), self.B, self.per,
                                          self.code, self.stream())
         _lib.check(rc, "cg_direction")
 
 
 def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, max_iters: int = 1000,
-       check_every: int = 4, graph: bool = False, ridge_param: float = 0.0, compact: float = 0.5) -> CGResult:
+       check_every: int = 4, graph: bool = False, ridge_param: float = 0.0, compact: float = 0.5,
+       precond=None, residuals: bool = True) -> CGResult:
     """Batched CG for (A^T A + 4 ridge_param I) x = A^T b; b: CUDA tensor
     (B, 4, 2n-1, n).
 
@@ -117,16 +145,19 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
     `compact` of the images still iterating are active (checked every
     `check_every` iterations), the finished ones are written out and the
     batch shrinks to the active ones, so the work follows the iterations each
-    image needs rather than the slowest image's (0 disables)."""
+    image needs rather than the slowest image's (0 disables).  `precond`:
+    preconditioner for PCG (see the module docstring).  `residuals=False`
+    skips recomputing the reported residuals (the fields are then None;
+    ``residuals_of`` computes them later)."""
     if not (isinstance(b, torch.Tensor) and b.is_cuda and b.ndim == 4):
         raise TypeError("cg expects a CUDA tensor of shape (B, 4, 2n-1, n)")
     if ridge_param < 0:
         raise ValueError("ridge_param must be non-negative")
-    st = _State(b, x0, 4.0 * float(ridge_param))
+    st = _State(b, x0, 4.0 * float(ridge_param), precond)
     thr2 = st.rhs2 * (tol * tol)
-    st.active.copy_((st.rs > thr2).to(torch.int32))
+    st.active.copy_((st.rr > thr2).to(torch.int32))
     B_full = st.B
-    rhs_full, rhs2_full = st.rhs, st.rhs2
+    rhs_full = st.rhs
     x_full = st.x
     iters_full = torch.zeros(B_full, dtype=torch.int32, device=st.dev)
     idx = torch.arange(B_full, device=st.dev)
@@ -135,15 +166,22 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
     g = None
     while k < max_iters:
         if graph and g is None and k >= 1:
+            # Capture on a side stream with the graph's own memory pool
+            # (capture_begin/end directly: the torch.cuda.graph context
+            # manager also runs the Python garbage collector and empties the
+            # allocator cache, which costs several iterations' time here).
             s = torch.cuda.Stream(device=st.dev)
             s.wait_stream(torch.cuda.current_stream(st.dev))
             with torch.cuda.stream(s):
                 st.iterate(thr2)  # warm the capture stream's allocator
                 k += 1
+                g = torch.cuda.CUDAGraph()
+                g.capture_begin()
+                try:
+                    st.iterate(thr2)
+                finally:
+                    g.capture_end()
             torch.cuda.current_stream(st.dev).wait_stream(s)
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                st.iterate(thr2)
             # capture does not execute; the first replay below runs it
         steps = min(check_every, max_iters - k)
         for _ in range(steps):
@@ -174,13 +212,31 @@ def cg(b: torch.Tensor, x0: torch.Tensor | None = None, *, tol: float = 1e-4, ma
         iters_full.index_copy_(0, idx, st.iters)
     else:
         iters_full = st.iters.clone()
-    # Recompute the reported residuals from scratch.
-    st.B = B_full
-    st.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(B_full), dtype=torch.uint8, device=st.dev)
-    res_n = normal_op(x_full, st.lam) - rhs_full
-    ax = _adrt(x_full)
-    dr = ax - b
-    normal_residual = torch.sqrt(st.dot(res_n, res_n) / rhs2_full)
-    nb = (b.reshape(B_full, -1).double() ** 2).sum(1)
-    data_residual = torch.sqrt((dr.reshape(B_full, -1).double() ** 2).sum(1) / nb)
+    if not residuals:
+        return CGResult(x_full, iters_full, None, None, k)
+    normal_residual, data_residual = residuals_of(b, x_full, ridge_param, rhs_full)
     return CGResult(x_full, iters_full, normal_residual, data_residual, k)
+
+
+def residuals_of(b: torch.Tensor, x: torch.Tensor, ridge_param: float = 0.0, rhs: torch.Tensor | None = None):
+    """(||A^T b - (A^T A + 4 ridge_param I) x|| / ||A^T b||, ||Ax - b|| / ||b||)
+    per image, recomputed from scratch (float64 sums); `rhs`: A^T b if known."""
+    B = b.shape[0]
+    if rhs is None:
+        rhs = _adjoint(b.contiguous())
+    res_n = normal_op(x, 4.0 * float(ridge_param)) - rhs
+    ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(B), dtype=torch.uint8, device=b.device)
+
+    def dot(u, v):
+        out = torch.empty(B, dtype=torch.float64, device=b.device)
+        rc = _lib.load().adrt_gb300_batched_dot(u.data_ptr(), v.data_ptr(), out.data_ptr(), B, u[0].numel(),
+                                               float_code(u), ws.data_ptr(),
+                                               torch.cuda.current_stream(b.device).cuda_stream)
+        _lib.check(rc, "batched_dot")
+        return out
+
+    normal_residual = torch.sqrt(dot(res_n, res_n) / dot(rhs, rhs))
+    dr = _adrt(x) - b
+    nb = (b.reshape(B, -1).double() ** 2).sum(1)
+    data_residual = torch.sqrt((dr.reshape(B, -1).double() ** 2).sum(1) / nb)
+    return normal_residual, data_residual

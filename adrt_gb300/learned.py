@@ -484,9 +484,11 @@ def train(net: PreconditionerNet, b: torch.Tensor, x_cg: torch.Tensor, *, epochs
 
 
 def learned_cg(net: PreconditionerNet, b: torch.Tensor, *, tol: float = 1e-4, max_iters: int = 1000,
-               graph: bool = True, check_every: int = 4):
-    """CG from the network's starting image; same stopping rule as plain CG."""
+               graph: bool = True, check_every: int = 4, precond=None):
+    """CG from the network's starting image (preconditioned CG with
+    `precond`); same stopping rule as plain CG."""
     from . import cg as cgmod
 
     x0 = net.predict(b)
-    return cgmod.cg(b, x0=x0, tol=tol, max_iters=max_iters, graph=graph, check_every=check_every)
+    return cgmod.cg(b, x0=x0, tol=tol, max_iters=max_iters, graph=graph, check_every=check_every,
+                    precond=precond)

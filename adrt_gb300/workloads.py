@@ -8,8 +8,8 @@ stream, after warm-up), images per second and the algorithmic bandwidth
 and as the command line under a profiler.
 
 Ops: adrt, bdrt, iadrt, adjoint, adrt_step, bdrt_step, fmg_restriction,
-fmg_prolongation, fmg_highpass, iadrt_fmg, ragged, cg, net_forward,
-net_train.
+fmg_prolongation, fmg_highpass, iadrt_fmg, ragged, cg, pcg, precond,
+net_forward, net_train.
 """
 
 from __future__ import annotations
@@ -21,7 +21,7 @@ import sys
 import torch
 
 OPS = ("adrt", "bdrt", "iadrt", "adjoint", "adrt_step", "bdrt_step", "fmg_restriction", "fmg_prolongation",
-       "fmg_highpass", "iadrt_fmg", "ragged", "cg", "net_forward", "net_train")
+       "fmg_highpass", "iadrt_fmg", "ragged", "cg", "pcg", "precond", "net_forward", "net_train")
 
 
 def _setup(op: str, n: int, batch: int, dtype, dev):
@@ -70,12 +70,19 @@ def _setup(op: str, n: int, batch: int, dtype, dev):
         imgs = ragged_phantoms(batch, seed=0, device=dev, dtype=dtype)
         nbytes = sum(es * (m.shape[-1] ** 2 + 4 * m.shape[-1] * (2 * m.shape[-1] - 1)) for m in imgs)
         return (lambda: adrt_ragged(imgs)), nbytes, batch
-    if op == "cg":
+    if op in ("cg", "pcg"):
         from adrt_gb300 import cg as cgmod
+        from adrt_gb300 import precond
 
         xt = ellipse_phantoms(batch, n, seed=0, device=dev, dtype=dtype)
         b = adrt.adrt(xt)
-        return (lambda: cgmod.cg(b, tol=1e-4, max_iters=200, graph=True)), 0, batch
+        M = precond.fit(n, h=4, samples=8, seed=0, device=dev, dtype=dtype) if op == "pcg" else None
+        return (lambda: cgmod.cg(b, tol=1e-4, max_iters=200, graph=True, precond=M)), 0, batch
+    if op == "precond":
+        from adrt_gb300 import precond
+
+        M = precond.ConvPreconditioner(sum(precond.basis(4)))
+        return (lambda: M.apply(img)), es * batch * 2 * n * n, batch
     if op in ("net_forward", "net_train"):
         from adrt_gb300.learned import PreconditionerNet
 

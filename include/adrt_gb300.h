@@ -288,6 +288,17 @@ int adrt_gb300_cg_direction(void *p, const void *r, const double *rs_new, double
  * (A^T A + lambda I) x of docs/examples.tomography.md:63-76. */
 int adrt_gb300_axpy(double alpha, const void *x, void *y, int64_t count, int dtype, void *stream);
 
+/* CG preconditioner (no reference counterpart): y = K * x per n x n image of
+ * a batch, a "same"-size 2-D convolution with zero padding; K is
+ * (2h+1) x (2h+1), 0 <= h <= 7, row-major, given as float64 values in HOST
+ * memory (they are copied into the launch, so a captured CUDA graph keeps
+ * them).  Point-symmetric K gives a symmetric operator; positive definite
+ * when K's symbol is positive at every frequency.  x and y: device arrays of
+ * batch * n * n elements of `dtype`, not overlapping; batch <= 65535,
+ * n <= 32768. */
+int adrt_gb300_precond_conv(const void *x, void *y, int64_t batch, int64_t n, const double *weights, int h,
+                            int dtype, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
