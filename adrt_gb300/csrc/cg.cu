@@ -1,10 +1,15 @@
 // Batched conjugate-gradient vector kernels for the ADRT normal equations.
 //
 // Every image of a batch runs its own CG recurrence; scalars (dot products,
-// alpha, beta) are per image and accumulated in float64 in a fixed order
-// (fixed grid, fixed per-thread stride, fixed shared-memory tree), so results
-// do not depend on scheduling.  An image whose `active` flag is 0 is frozen:
-// its alpha is 0 and its direction is left unchanged.
+// alpha, beta) are per image.  A dot product is reduced in a fixed order:
+// each thread sums its strided slice in the data type (products and sums
+// rounded separately, no FMA), the per-thread sums are combined in float64
+// by a fixed warp-shuffle tree, then across the block's warps and the
+// image's blocks in index order -- so results do not depend on scheduling.
+// (float64 arithmetic is slow on this GPU: the per-element work stays in the
+// data type; float64 data therefore accumulates in float64 throughout.)
+// An image whose `active` flag is 0 is frozen: its alpha is 0 and its
+// direction is left unchanged.
 #include "common.cuh"
 
 namespace adrtg {
@@ -12,27 +17,30 @@ namespace adrtg {
 constexpr int kDotThreads = 256;
 constexpr int kDotBlocksPerImage = 32;
 
+// Sum over the block in a fixed order: shuffle tree within each warp, then
+// the warps' sums in warp order.
 __device__ __forceinline__ double block_sum(double v, double *sh) {
-  sh[threadIdx.x] = v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
   __syncthreads();
-  for (int s = kDotThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + s]);
-    __syncthreads();
-  }
-  return sh[0];
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kDotThreads / 32; ++w) s = __dadd_rn(s, sh[w]);
+  return s;
 }
 
 // partial[img][blk] = sum over the block's strided slice of a*b.
 template <typename T>
-__global__ void dot_partial_kernel(const T *__restrict__ a, const T *__restrict__ b, i64 per,
-                                   double *partial) {
-  __shared__ double sh[kDotThreads];
+__global__ void __launch_bounds__(kDotThreads) dot_partial_kernel(const T *__restrict__ a, const T *__restrict__ b,
+                                                                 i64 per, double *partial) {
+  __shared__ double sh[kDotThreads / 32];
   const int img = blockIdx.y, blk = blockIdx.x;
   const T *pa = a + (i64)img * per, *pb = b + (i64)img * per;
-  double acc = 0.0;
+  T acc = T(0);
   for (i64 i = (i64)blk * kDotThreads + threadIdx.x; i < per; i += (i64)kDotBlocksPerImage * kDotThreads)
-    acc = __dadd_rn(acc, __dmul_rn((double)pa[i], (double)pb[i]));
-  const double s = block_sum(acc, sh);
+    acc = add_rn(acc, mul_rn(pa[i], pb[i]));
+  const double s = block_sum((double)acc, sh);
   if (threadIdx.x == 0) partial[img * kDotBlocksPerImage + blk] = s;
 }
 
@@ -47,17 +55,18 @@ __global__ void dot_final_kernel(const double *partial, double *out, int batch) 
 // alpha = rs / pAp (0 if frozen or pAp == 0); x += alpha p; r -= alpha Ap;
 // partial sums of r*r for rs_new.
 template <typename T>
-__global__ void cg_update_kernel(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
-                                 const T *__restrict__ Ap, const double *rs, const double *pAp,
-                                 const int *active, i64 per, double *partial) {
-  __shared__ double sh[kDotThreads];
+__global__ void __launch_bounds__(kDotThreads) cg_update_kernel(T *__restrict__ x, T *__restrict__ r,
+                                                               const T *__restrict__ p, const T *__restrict__ Ap,
+                                                               const double *rs, const double *pAp,
+                                                               const int *active, i64 per, double *partial) {
+  __shared__ double sh[kDotThreads / 32];
   const int img = blockIdx.y, blk = blockIdx.x;
   const double den = pAp[img];
   const bool on = active[img] != 0 && den != 0.0;
   const T alpha = on ? (T)(rs[img] / den) : T(0);
   T *px = x + (i64)img * per, *pr = r + (i64)img * per;
   const T *pp = p + (i64)img * per, *pAp_ = Ap + (i64)img * per;
-  double acc = 0.0;
+  T acc = T(0);
   for (i64 i = (i64)blk * kDotThreads + threadIdx.x; i < per; i += (i64)kDotBlocksPerImage * kDotThreads) {
     T rv = pr[i];
     if (on) {
@@ -65,9 +74,9 @@ __global__ void cg_update_kernel(T *__restrict__ x, T *__restrict__ r, const T *
       rv = sub_rn(rv, mul_rn(alpha, pAp_[i]));
       pr[i] = rv;
     }
-    acc = __dadd_rn(acc, __dmul_rn((double)rv, (double)rv));
+    acc = add_rn(acc, mul_rn(rv, rv));
   }
-  const double s = block_sum(acc, sh);
+  const double s = block_sum((double)acc, sh);
   if (threadIdx.x == 0) partial[img * kDotBlocksPerImage + blk] = s;
 }
 

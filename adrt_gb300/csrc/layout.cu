@@ -143,6 +143,36 @@ __global__ void quad_sum_kernel(const T *__restrict__ y, T *__restrict__ out, I 
   }
 }
 
+// The same sum for n >= 32 on 32 x 32 output tiles: quadrants 0 and 3 are
+// read along their rows (coalesced) into shared memory and taken transposed
+// from there; quadrants 1 and 2 are read directly.  Same operand order.
+template <typename T>
+__global__ void __launch_bounds__(256) quad_sum_tiled_kernel(const T *__restrict__ y, T *__restrict__ out,
+                                                             unsigned n) {
+  __shared__ T t0[32][33], t3[32][33];
+  const unsigned C = 2 * n - 1;
+  const unsigned i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const T *yb = y + (size_t)blockIdx.z * 4 * C * n;
+  const unsigned tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (unsigned k = 0; k < 4; ++k) {
+    const unsigned jj = ty + 8 * k;
+    const unsigned srow = n - 1 - (j0 + jj);
+    t0[jj][tx] = yb[srow * n + (i0 + tx)];                          // quadrant 0: (n-1-j, i)
+    t3[jj][tx] = yb[3 * (size_t)C * n + srow * n + (n - 1 - (i0 + tx))];  // quadrant 3: (n-1-j, n-1-i)
+  }
+  __syncthreads();
+  T *ob = out + (size_t)blockIdx.z * n * n;
+#pragma unroll
+  for (unsigned k = 0; k < 4; ++k) {
+    const unsigned ii = ty + 8 * k;
+    const unsigned i = i0 + ii, j = j0 + tx;
+    T s = add_rn(t0[tx][ii], yb[(size_t)C * n + (n - 1 - i) * n + j]);
+    s = add_rn(s, yb[2 * (size_t)C * n + i * n + j]);
+    ob[i * n + j] = add_rn(s, t3[tx][ii]);
+  }
+}
+
 template <typename W>
 __global__ void init_kernel_u32(const W *__restrict__ in, W *__restrict__ out, unsigned batch, unsigned n) {
   init_body<W, unsigned>(in, out, batch, n);
@@ -221,6 +251,11 @@ template <typename T>
 int quad_sum_launch(const T *y, T *out, i64 batch, i64 n, cudaStream_t st) {
   const i64 total = batch * n * n;
   const int lg = num_iters(n);
+  if (n >= 32 && n <= 32768 && batch <= 65535) {
+    const unsigned t = (unsigned)(n / 32);
+    quad_sum_tiled_kernel<T><<<dim3(t, t, (unsigned)batch), 256, 0, st>>>(y, out, (unsigned)n);
+    return launch_status();
+  }
   if (total * 8 < (i64(1) << 32))
     quad_sum_kernel<T, unsigned><<<grid_l(total), 256, 0, st>>>(y, out, (unsigned)total, (unsigned)n, lg);
   else

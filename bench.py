@@ -335,7 +335,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--n", type=int, default=1024)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (built-in launch configuration)")
@@ -422,19 +422,17 @@ def main():
         # is alive while the next one runs, so the cache settles on two),
         # which takes seconds for 8.6 GB results.
         # At least four calls (the first two allocate, the third still
-        # settles), then until two in a row agree within 10 %.
-        prev = None
+        # settles), then until three in a row agree within 10 %.
         warm_ms = []
-        for i in range(10):
+        for i in range(16):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             yh = adrt.adrt(xh)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
             warm_ms.append(round(dt * 1e3, 1))
-            if i >= 3 and abs(dt - prev) <= 0.1 * prev:
+            if i >= 3 and max(warm_ms[-3:]) <= 1.1 * min(warm_ms[-3:]):
                 break
-            prev = dt
         barrier()
         torch.cuda.synchronize()
         call_ms = []

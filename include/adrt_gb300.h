@@ -270,7 +270,9 @@ int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void 
 /* Bytes of workspace the CG kernels need for `batch` images. */
 size_t adrt_gb300_cg_workspace_size(int64_t batch);
 
-/* out[i] = sum_k a[i,k] * b[i,k] (float64). */
+/* out[i] = sum_k a[i,k] * b[i,k], returned in float64: per-thread partial
+ * sums in the data type over a fixed strided slice, combined in float64 in a
+ * fixed order (deterministic). */
 int adrt_gb300_batched_dot(const void *a, const void *b, double *out, int64_t batch, int64_t per,
                            int dtype, void *workspace, void *stream);
 
