@@ -118,38 +118,51 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   // the reference's +0 padding.  Offsets inside one image or quadrant are
   // 32-bit (n <= 32768, checked by the host).
   const unsigned un = (unsigned)n;
+  const int lr = threadIdx.x % TL::TPR;
   if (FIRST) {
     const T *img = static_cast<const T *>(args.in) + (size_t)b * un * un;
-    const bool col_major = (q == 1 || q == 2);
+    if (q == 1 || q == 2) {
+      // Columns of the image: consecutive threads take consecutive rows i
+      // (adjacent in memory).  Quadrant 1 runs up the column, 2 down.
 #pragma unroll 4
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
-      int i, u;
-      if (col_major) { i = idx % ROWS; u = idx / ROWS; }
-      else { i = idx / TWP; u = idx % TWP; }
-      const int ref = (int)tbase + u;  // a' == 0 in the first pass
-      const unsigned R0 = (unsigned)r * ROWS + i;
-      T v = ref < 0 ? T(-0.0) : T(0);
-      if (ref >= 0 && ref < (int)un) {
-        const unsigned c = (unsigned)ref;
-        switch (q) {
-          case 0: v = img[R0 * un + (un - 1 - c)]; break;
-          case 1: v = img[(un - 1 - c) * un + R0]; break;
-          case 2: v = img[c * un + R0]; break;
-          default: v = img[(un - 1 - R0) * un + (un - 1 - c)]; break;
+      for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
+        const int i = idx % ROWS, u = idx / ROWS;
+        const int ref = (int)tbase + u;  // a' == 0 in the first pass
+        T v = ref < 0 ? T(-0.0) : T(0);
+        if (ref >= 0 && ref < (int)un) {
+          const unsigned c = (unsigned)ref, row = q == 1 ? un - 1 - c : c;
+          v = img[row * un + (unsigned)r * ROWS + i];
+        }
+        buf0[i * RS + u] = v;
+      }
+    } else {
+      // Rows of the image read from their right end (quadrant 0 row R0,
+      // quadrant 3 row n-1-R0).
+      for (int i = threadIdx.x / TL::TPR; i < ROWS; i += TL::ROW_STEP) {
+        const unsigned R0 = (unsigned)r * ROWS + i;
+        const T *rowp = img + (q == 0 ? R0 : un - 1 - R0) * un + (un - 1);
+#pragma unroll 4
+        for (int u = lr; u < TWP; u += TL::TPR) {
+          const int ref = (int)tbase + u;
+          T v = ref < 0 ? T(-0.0) : T(0);
+          if (ref >= 0 && ref < (int)un) v = rowp[-ref];
+          buf0[i * RS + u] = v;
         }
       }
-      buf0[i * RS + u] = v;
     }
   } else {
     const T *src = static_cast<const T *>(args.in) + ((size_t)b * 4 + q) * un * (size_t)C;
     const unsigned row0 = (unsigned)r * ROWS * (unsigned)A_in + (unsigned)ap;
+    for (int i = threadIdx.x / TL::TPR; i < ROWS; i += TL::ROW_STEP) {
+      const T *rowp = src + (size_t)(row0 + (unsigned)i * (unsigned)A_in) * (unsigned)C;
+      const int rb = (int)tbase - (int)ap * i;
 #pragma unroll 4
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
-      const int i = idx / TWP, u = idx % TWP;
-      const int ref = (int)tbase + u - (int)ap * i;
-      T v = ref < 0 ? T(-0.0) : T(0);
-      if (ref >= 0 && ref < (int)C) v = ld_l2(&src[(row0 + (unsigned)i * (unsigned)A_in) * (unsigned)C + (unsigned)ref]);
-      buf0[i * RS + u] = v;
+      for (int u = lr; u < TWP; u += TL::TPR) {
+        const int ref = rb + u;
+        T v = ref < 0 ? T(-0.0) : T(0);
+        if (ref >= 0 && ref < (int)C) v = ld_l2(&rowp[ref]);
+        buf0[i * RS + u] = v;
+      }
     }
   }
   __syncthreads();
@@ -157,7 +170,6 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   // ---- S stages in shared memory: row m*2A + 2li + p of the output is
   // row 2m*A + li plus row (2m+1)*A + li shifted by li + p.
   T *cur = buf0, *nxt = buf1;
-  const int lr = threadIdx.x % TL::TPR;
 #pragma unroll
   for (int j = 0; j < S; ++j) {
     const int Al_in = 1 << j, Al_out = 2 << j;

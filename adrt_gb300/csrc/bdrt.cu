@@ -116,12 +116,14 @@ bwd_pass_kernel(BwdPassArgs args) {
     }
   } else {
     const T *src = static_cast<const T *>(args.in) + qoff + ((size_t)ap * ROWS * R_hi + r) * C + c0;
+    for (int l = threadIdx.x / TL::TPR; l < ROWS; l += TL::ROW_STEP) {
+      const T *rowp = src + (size_t)l * R_hi * (unsigned)C;
 #pragma unroll 4
-    for (int idx = threadIdx.x; idx < ROWS * TWP; idx += NT) {
-      const int l = idx / TWP, u = idx % TWP;
-      T v = T(0);
-      if (c0 + u < C) v = src[(unsigned)l * R_hi * (unsigned)C + u];
-      buf0[l * RS + u] = v;
+      for (int u = threadIdx.x % TL::TPR; u < TWP; u += TL::TPR) {
+        T v = T(0);
+        if (c0 + u < C) v = rowp[u];
+        buf0[l * RS + u] = v;
+      }
     }
   }
   __syncthreads();
@@ -180,11 +182,14 @@ bwd_pass_kernel(BwdPassArgs args) {
     }
   } else {
     T *dst = static_cast<T *>(args.out) + qoff + ((size_t)ap * R_lo + r * ROWS) * C;
+    for (int i = threadIdx.x / TL::TPR; i < ROWS; i += TL::ROW_STEP) {
+      T *rowp = dst + (size_t)i * (unsigned)C;
+      const int cb = c0 - (int)ap * i;
 #pragma unroll 4
-    for (int idx = threadIdx.x; idx < ROWS * W; idx += NT) {
-      const int i = idx / W, w = idx % W;
-      const int c = c0 + w - (int)ap * i;
-      if (c >= 0 && c < C) dst[(unsigned)i * (unsigned)C + (unsigned)c] = cur[i * RS + w];
+      for (int w = threadIdx.x % TL::TPR; w < W; w += TL::TPR) {
+        const int c = cb + w;
+        if (c >= 0 && c < C) rowp[c] = cur[i * RS + w];
+      }
     }
   }
 }
