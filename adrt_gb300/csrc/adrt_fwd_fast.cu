@@ -61,6 +61,17 @@ __device__ __forceinline__ void st8(float *p, const float (&v)[8]) {
                : "memory");
 }
 
+// Two float32 adds in one packed instruction: d0 = a0 + b0, d1 = a1 + b1,
+// each rounded to nearest like add_rn (add.rn.f32x2 rounds per element).
+// Used where both operands of two neighbouring positions are adjacent
+// (butterfly shifts that are even).
+__device__ __forceinline__ void add_rn2(float a0, float a1, float b0, float b1, float &d0, float &d1) {
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d0), "=f"(d1)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 // Value of `cur` held by the lane D below (the previous chunk).  Lanes whose
 // previous chunk was handled in the previous iteration (lane < D) receive the
 // `saved` copy from lanes 32-D..31.
@@ -157,10 +168,13 @@ __device__ __forceinline__ void group1_compute(const float (&m)[4][4], float (&o
   saved.m3 = m[3][3];
   float s0[2][2][4];  // [pair][p][k]
 #pragma unroll
+  for (int k = 0; k < 4; k += 2) {
+    add_rn2(m[0][k], m[0][k + 1], m[1][k], m[1][k + 1], s0[0][0][k], s0[0][0][k + 1]);
+    add_rn2(m[2][k], m[2][k + 1], m[3][k], m[3][k + 1], s0[1][0][k], s0[1][0][k + 1]);
+  }
+#pragma unroll
   for (int k = 0; k < 4; ++k) {
-    s0[0][0][k] = add_rn(m[0][k], m[1][k]);
     s0[0][1][k] = add_rn(m[0][k], k ? m[1][k - 1] : pm1);
-    s0[1][0][k] = add_rn(m[2][k], m[3][k]);
     s0[1][1][k] = add_rn(m[2][k], k ? m[3][k - 1] : pm3);
   }
   // stage 1: combo 0 (pair 0) + combo 1 (pair 1) shifted by li + p.
@@ -182,11 +196,14 @@ __device__ __forceinline__ void group1_compute(const float (&m)[4][4], float (&o
     ext1[k + 2] = s0[1][1][k];
   }
 #pragma unroll
+  for (int k = 0; k < 4; k += 2) {
+    add_rn2(s0[0][0][k], s0[0][0][k + 1], ext0[k + 2], ext0[k + 3], o[0][k], o[0][k + 1]);  // li=0, p=0
+    add_rn2(s0[0][1][k], s0[0][1][k + 1], ext1[k], ext1[k + 1], o[3][k], o[3][k + 1]);      // li=1, p=1
+  }
+#pragma unroll
   for (int k = 0; k < 4; ++k) {
-    o[0][k] = add_rn(s0[0][0][k], ext0[k + 2]);      // li=0, p=0
     o[1][k] = add_rn(s0[0][0][k], ext0[k + 1]);      // li=0, p=1
     o[2][k] = add_rn(s0[0][1][k], ext1[k + 1]);      // li=1, p=0
-    o[3][k] = add_rn(s0[0][1][k], ext1[k]);          // li=1, p=1
   }
 }
 
@@ -393,10 +410,10 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
   for (int P = 0; P < 4; ++P) {
     const float pv = __shfl_up_sync(FULL, r[2 * P + 1][7], 1);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      t0[P][0][k] = add_rn(r[2 * P][k], r[2 * P + 1][k]);
-      t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
-    }
+    for (int k = 0; k < 8; k += 2)
+      add_rn2(r[2 * P][k], r[2 * P][k + 1], r[2 * P + 1][k], r[2 * P + 1][k + 1], t0[P][0][k], t0[P][0][k + 1]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
   }
   // stage b: combos (2Q, 2Q+1), li in {0,1}, shift li + p.
   float t1[2][4][8];
@@ -412,8 +429,15 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const int sh = li + p;
+        if (sh % 2 == 0) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) t1[Q][2 * li + p][k] = add_rn(t0[2 * Q][li][k], ext[k + 2 - sh]);
+          for (int k = 0; k < 8; k += 2)
+            add_rn2(t0[2 * Q][li][k], t0[2 * Q][li][k + 1], ext[k + 2 - sh], ext[k + 3 - sh], t1[Q][2 * li + p][k],
+                    t1[Q][2 * li + p][k + 1]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) t1[Q][2 * li + p][k] = add_rn(t0[2 * Q][li][k], ext[k + 2 - sh]);
+        }
       }
     }
   }
@@ -428,8 +452,15 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
       const int sh = li + p;
+      if (sh % 2 == 0) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) out[2 * li + p][k] = add_rn(t1[0][li][k], ext[k + 4 - sh]);
+        for (int k = 0; k < 8; k += 2)
+          add_rn2(t1[0][li][k], t1[0][li][k + 1], ext[k + 4 - sh], ext[k + 5 - sh], out[2 * li + p][k],
+                  out[2 * li + p][k + 1]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) out[2 * li + p][k] = add_rn(t1[0][li][k], ext[k + 4 - sh]);
+      }
     }
   }
 }
