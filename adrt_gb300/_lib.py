@@ -69,6 +69,8 @@ SIGNATURES = {
     "adrt_gb300_elementwise": [_int, _v, _v, _v, _i64, _int, _v],
     "adrt_gb300_sumsq_workspace_size": [],
     "adrt_gb300_sumsq": [_v, _i64, _int, _v, _v, _v],
+    "adrt_gb300_sumsq_batched_workspace_size": [_i64],
+    "adrt_gb300_sumsq_batched": [_v, _i64, _i64, _int, _v, _v, _v],
     "adrt_gb300_cg_workspace_size": [_i64],
     "adrt_gb300_ragged_workspace_size": [_v, _i64, _int, ctypes.POINTER(_sz)],
     "adrt_gb300_adrt_ragged": [_v, _v, _v, _i64, _int, _v, _sz, _v],
@@ -105,6 +107,7 @@ _RESTYPES = {
     "adrt_gb300_tune_reset": None,
     "adrt_gb300_status_string": ctypes.c_char_p,
     "adrt_gb300_sumsq_workspace_size": _sz,
+    "adrt_gb300_sumsq_batched_workspace_size": _sz,
     "adrt_gb300_launch_count": ctypes.c_uint64,
     "adrt_gb300_cg_workspace_size": _sz,
 }

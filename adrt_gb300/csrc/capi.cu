@@ -15,7 +15,7 @@ template <typename T> int fmg_highpass_launch(const T *, T *, i64, i64, i64, cud
 template <typename T> int quad_sum_launch(const T *, T *, i64, i64, cudaStream_t);
 template <typename T> int fmg_correction_launch(const T *, T *, i64, i64, cudaStream_t);
 template <typename T> int binary_launch(const T *, const T *, T *, i64, int, cudaStream_t);
-template <typename T> int sumsq_launch(const T *, i64, double *, void *, cudaStream_t);
+template <typename T> int sumsq_launch(const T *, i64, double *, void *, cudaStream_t, i64);
 size_t sumsq_workspace_bytes();
 unsigned *fast_error_word();
 size_t ragged_workspace_bytes(const int64_t *, i64, size_t, int *);
@@ -279,8 +279,24 @@ int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void 
   if ((rc = check_dtype(dtype))) return rc;
   if (count < 0) return ADRT_GB300_ERR_SHAPE;
   return DISPATCH(dtype,
-                  sumsq_launch<float>((const float *)a, count, out, ws, S(stream)),
-                  sumsq_launch<double>((const double *)a, count, out, ws, S(stream)));
+                  sumsq_launch<float>((const float *)a, count, out, ws, S(stream), 1),
+                  sumsq_launch<double>((const double *)a, count, out, ws, S(stream), 1));
+}
+
+size_t adrt_gb300_sumsq_batched_workspace_size(int64_t batch) {
+  return batch > 0 ? sumsq_workspace_bytes() * (size_t)batch : 0;
+}
+
+int adrt_gb300_sumsq_batched(const void *a, int64_t batch, int64_t count, int dtype, double *out, void *ws,
+                             void *stream) {
+  int rc;
+  if (!a || !out || !ws) return ADRT_GB300_ERR_NULL;
+  if ((rc = check_dtype(dtype))) return rc;
+  if (count < 0 || batch < 1) return ADRT_GB300_ERR_SHAPE;
+  if (batch > 65535) return ADRT_GB300_ERR_TOO_LARGE;
+  return DISPATCH(dtype,
+                  sumsq_launch<float>((const float *)a, count, out, ws, S(stream), batch),
+                  sumsq_launch<double>((const double *)a, count, out, ws, S(stream), batch));
 }
 
 }  // extern "C"

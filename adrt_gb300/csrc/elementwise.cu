@@ -48,9 +48,13 @@ __global__ void binary_kernel(const T *__restrict__ a, const T *__restrict__ b, 
 constexpr int kSqThreads = 256;
 constexpr int kSqBlocks = 512;
 
+// blockIdx.y selects an image of `count` elements (a batch of sums computed
+// with exactly the single-array partition, image by image).
 template <typename T>
 __global__ void sumsq_partial_kernel(const T *__restrict__ a, i64 count, double *partial) {
   __shared__ double sh[kSqThreads];
+  a += (i64)blockIdx.y * count;
+  partial += (size_t)blockIdx.y * kSqBlocks;
   double acc = 0.0;
   for (i64 i = blockIdx.x * (i64)kSqThreads + threadIdx.x; i < count; i += (i64)kSqBlocks * kSqThreads) {
     const double v = (double)a[i];
@@ -67,6 +71,8 @@ __global__ void sumsq_partial_kernel(const T *__restrict__ a, i64 count, double 
 
 __global__ void sumsq_final_kernel(const double *partial, double *out) {
   __shared__ double sh[kSqBlocks];
+  partial += (size_t)blockIdx.x * kSqBlocks;
+  out += blockIdx.x;
   for (int i = threadIdx.x; i < kSqBlocks; i += blockDim.x) sh[i] = partial[i];
   __syncthreads();
   for (int s = kSqBlocks / 2; s > 0; s >>= 1) {
@@ -104,17 +110,17 @@ int binary_launch(const T *a, const T *b, T *out, i64 count, int op, cudaStream_
 size_t sumsq_workspace_bytes() { return sizeof(double) * kSqBlocks; }
 
 template <typename T>
-int sumsq_launch(const T *a, i64 count, double *out, void *ws, cudaStream_t st) {
+int sumsq_launch(const T *a, i64 count, double *out, void *ws, cudaStream_t st, i64 batch) {
   double *partial = static_cast<double *>(ws);
-  sumsq_partial_kernel<T><<<kSqBlocks, kSqThreads, 0, st>>>(a, count, partial);
-  sumsq_final_kernel<<<1, 256, 0, st>>>(partial, out);
+  sumsq_partial_kernel<T><<<dim3(kSqBlocks, (unsigned)batch), kSqThreads, 0, st>>>(a, count, partial);
+  sumsq_final_kernel<<<(unsigned)batch, 256, 0, st>>>(partial, out);
   return launch_status();
 }
 
 #define INST(T)                                                                   \
   template int fmg_correction_launch<T>(const T *, T *, i64, i64, cudaStream_t);  \
   template int binary_launch<T>(const T *, const T *, T *, i64, int, cudaStream_t); \
-  template int sumsq_launch<T>(const T *, i64, double *, void *, cudaStream_t);
+  template int sumsq_launch<T>(const T *, i64, double *, void *, cudaStream_t, i64);
 INST(float)
 INST(double)
 #undef INST

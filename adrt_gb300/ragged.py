@@ -87,7 +87,17 @@ def iadrt_ragged(arrays):
 
 
 def iadrt_fmg_ragged(arrays, max_iters=None):
-    """Full-multigrid inverse of each array (the reference's iadrt_fmg takes no batch)."""
-    from . import iadrt_fmg
+    """Full-multigrid inverse of each array; arrays of one size iterate as a
+    batch (``iadrt_fmg_batched``), each image with iadrt_fmg's own stopping
+    rule and an identical result."""
+    from . import iadrt_fmg_batched
 
-    return [iadrt_fmg(a, max_iters=max_iters) for a in arrays]
+    groups = defaultdict(list)
+    for i, a in enumerate(arrays):
+        groups[int(a.shape[-1])].append(i)
+    out = [None] * len(arrays)
+    for n, idx in groups.items():
+        res = iadrt_fmg_batched(torch.stack([arrays[i] for i in idx]), max_iters=max_iters)
+        for k, i in enumerate(idx):
+            out[i] = res[k]
+    return out

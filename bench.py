@@ -287,6 +287,99 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
     return out
 
 
+def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
+    """The ragged workload: `count` float32 ellipse phantoms with sides drawn
+    from {32..1024} (weights .3/.25/.2/.15/.07/.03).  Forward ADRT in one
+    persistent launch, the exact inverse and the full-multigrid inverse
+    (both batched per size; each image keeps iadrt_fmg's own stopping rule)
+    on the first `fmg_sample` images.  Relative errors vs the input image
+    (for iadrt: the mean of its four truncated quadrants) are reported per size (the exact inverse is ill-conditioned in float32:
+    its error grows with n, as in the reference, which it matches bit for bit
+    in the tests)."""
+    import numpy as np
+
+    import adrt_gb300 as adrt
+    from adrt_gb300.data import ragged_phantoms
+    from adrt_gb300.ragged import adrt_ragged, iadrt_fmg_ragged, iadrt_ragged
+
+    imgs = ragged_phantoms(count, seed=0, device=dev)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) / reps
+
+    ys, t_fwd = timed(lambda: adrt_ragged(imgs), 3)
+    inv, t_inv = timed(lambda: iadrt_ragged(ys), 3)
+    sub = list(range(fmg_sample))
+    fmg, t_fmg = timed(lambda: iadrt_fmg_ragged([ys[i] for i in sub]), 1)
+
+    def rel(a, b):
+        return float((a.double() - b.double()).norm() / b.double().norm())
+
+    sizes = sorted({int(m.shape[-1]) for m in imgs})
+    # iadrt returns the (4, 2n-1, n) array whose truncated quadrants are four
+    # copies of the image; compare their mean with the input.
+    rec = [adrt.utils.truncate(v).mean(0) for v in inv]
+    err_inv = {str(n): float(np.median([rel(rec[i], imgs[i]) for i in range(count) if imgs[i].shape[-1] == n]))
+               for n in sizes}
+    err_fmg = {}
+    for n in sizes:
+        e = [rel(fmg[k], imgs[i]) for k, i in enumerate(sub) if imgs[i].shape[-1] == n]
+        if e:
+            err_fmg[str(n)] = float(np.median(e))
+    return {
+        "workload": f"{count} float32 ellipse phantoms, n from {{32..1024}} weights .3/.25/.2/.15/.07/.03",
+        "counts": {str(n): sum(1 for m in imgs if m.shape[-1] == n) for n in sizes},
+        "adrt_img_s": count / t_fwd,
+        "adrt_ms": 1e3 * t_fwd,
+        "iadrt_img_s": count / t_inv,
+        "iadrt_fmg_img_s": fmg_sample / t_fmg,
+        "iadrt_fmg_sample": fmg_sample,
+        "iadrt_rel_err_vs_input_median": err_inv,
+        "iadrt_fmg_rel_err_vs_input_median": err_fmg,
+    }
+
+
+def autograd_bench(torch, dev, batch=64, n=512, steps=5):
+    """Differentiable ADRT: loss = ||adrt(x) - y||^2 with y = adrt(phantom) +
+    N(0, (1e-3 max|y|)^2), batch 64 x 512^2 float32; forward + backward (the
+    hand-written adjoint kernel) per step, CUDA-event timed."""
+    from adrt_gb300 import autograd as ag
+    from adrt_gb300.data import ellipse_phantoms
+
+    xt = ellipse_phantoms(batch, n, seed=7, device=dev)
+    y = ag.adrt(xt)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    y = (y + 1e-3 * y.abs().amax() * torch.randn(y.shape, generator=g, device=dev)).detach()
+    x = torch.zeros_like(xt, requires_grad=True)
+
+    def step():
+        x.grad = None
+        loss = (ag.adrt(x) - y).pow(2).sum()
+        loss.backward()
+        return loss
+
+    for _ in range(3):
+        step()
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / steps
+    return {"workload": f"loss ||adrt(x) - y||^2, batch {batch} x {n}^2 float32, forward + backward",
+            "steps_s": 1.0 / t, "img_s": batch / t, "ms_per_step": 1e3 * t}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -483,6 +576,8 @@ def main():
         del y64, x64
 
     if not args.no_extras and rank == 0:
+        extras["autograd"] = autograd_bench(torch, dev)
+        extras["ragged"] = ragged_bench(torch, dev)
         extras["cg"] = cg_bench(torch, dev)
 
     peak, peak_src = load_peaks()

@@ -260,6 +260,14 @@ size_t adrt_gb300_sumsq_workspace_size(void);
 int adrt_gb300_sumsq(const void *a, int64_t count, int dtype, double *out, void *workspace,
                      void *stream);
 
+/* The same sum for each of `batch` consecutive arrays of `count` elements:
+ * out[i] (device double[batch]) equals adrt_gb300_sumsq of array i bit for
+ * bit.  workspace: adrt_gb300_sumsq_batched_workspace_size(batch) bytes.
+ * Used by the batched full-multigrid inverse (per-image stopping rule). */
+size_t adrt_gb300_sumsq_batched_workspace_size(int64_t batch);
+int adrt_gb300_sumsq_batched(const void *a, int64_t batch, int64_t count, int dtype, double *out,
+                             void *workspace, void *stream);
+
 /* ---- Batched conjugate gradient on the normal equations A^T A x = A^T b.
  * The reference documents this solve as a SciPy recipe
  * (docs/examples.cginverse.md:40-67); these kernels run its vector algebra for
