@@ -20,49 +20,54 @@ namespace adrtg {
 // Loads for a chain never depend on its running value, so each thread keeps
 // the operands of the next U rows in a register ring (slot u holds row
 // row0 - u): the latency of a load is hidden behind U serial steps instead of
-// stalling every step.  Threads are ordered so that the first n/2 of a plane
+// stalling every step.  U = 32 (float32) / 16 (float64) for n >= 1024, where
+// few chains run per SM and the deeper ring hides more latency (n = 1024,
+// batch 2: 1.9k img/s against 1.6k with 16); half that below, where more
+// chains are resident and the smaller register footprint wins (n = 256,
+// batch 64: 111k against 97k img/s).  Threads are ordered so that the first n/2 of a plane
 // run even-l chains and the rest odd-l chains: warps do not diverge between
 // the two recurrences.
-template <typename T> struct IadrtRing { static constexpr int U = sizeof(T) == 4 ? 16 : 8; };
 
 template <typename T>
 __device__ __forceinline__ T ld_or_zero(const T *p, bool ok) { return ok ? __ldg(p) : T(0); }
 
-template <typename T>
+// Index arithmetic is 32-bit: a plane holds n (2n-1) < 2^31 elements for the
+// sizes the host accepts (n <= 32768).
+template <typename T, int U>
 __global__ void __launch_bounds__(128)
-iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i64 n, int s) {
-  constexpr int U = IadrtRing<T>::U;
-  const i64 R = 2 * n - 1;
-  const i64 Cc = n >> s;           // input chains per l
-  const i64 C2 = Cc >> 1;          // output chains per l
-  const i64 half = n >> 1;         // even-l (and odd-l) chains per plane
+iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i64 n_, int s) {
+  const int n = (int)n_;
+  const int R = 2 * n - 1;
+  const int Cc = n >> s;           // input chains per l
+  const int C2 = Cc >> 1;          // output chains per l
+  const int half = n >> 1;         // even-l (and odd-l) chains per plane
   const i64 gid = blockIdx.x * (i64)blockDim.x + threadIdx.x;
   if (gid >= planes * n) return;
   const i64 plane = gid / n;
-  const i64 t = gid % n;
+  const int t = (int)(gid - plane * n);
   const bool odd = t >= half;
-  const i64 tt = odd ? t - half : t;
-  const i64 l = 2 * (tt / C2) + (odd ? 1 : 0), col = tt % C2;
-  const i64 ch = l * C2 + col;
-  const i64 pl = l >> 1;
-  const T *src = in + plane * R * n;
-  T *dst = out + plane * R * n;
-  const i64 e_ch = pl * Cc + 2 * col;
-  const i64 o_ch = e_ch + 1;
+  const int tt = odd ? t - half : t;
+  const int l = 2 * (tt / C2) + (odd ? 1 : 0), col = tt % C2;
+  const int ch = l * C2 + col;
+  const int pl = l >> 1;
+  const T *src = in + plane * (i64)R * n;
+  T *dst = out + plane * (i64)R * n;
+  const int e_ch = pl * Cc + 2 * col;
+  const int o_ch = e_ch + 1;
   T ea[U], oa[U];
   T prev = T(0);
   if (!odd) {
     // v = (0 + E[row]) - O[row + 1] + prev   (O and prev only if row + 1 < R)
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const i64 r = R - 1 - u;
+      const int r = R - 1 - u;
       ea[u] = ld_or_zero(src + r * n + e_ch, r >= 0);
       oa[u] = ld_or_zero(src + (r + 1) * n + o_ch, r >= 0 && r + 1 < R);
     }
-    for (i64 row0 = R - 1; row0 >= 0; row0 -= U) {
+    for (int row0 = R - 1; row0 >= 0; row0 -= U) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const i64 row = row0 - u;
+        const int row = row0 - u;
         if (row >= 0) {
           T v = add_rn(T(0), ea[u]);
           if (row + 1 < R) {
@@ -72,25 +77,25 @@ iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i6
           dst[row * n + ch] = v;
           prev = v;
         }
-        const i64 r = row - U;
+        const int r = row - U;
         ea[u] = ld_or_zero(src + r * n + e_ch, r >= 0);
         oa[u] = ld_or_zero(src + (r + 1) * n + o_ch, r >= 0);
       }
     }
   } else {
     // v = (0 + O[row + d]) - E[row + d]  (if row + d < R, else 0); v += prev (row + 1 < R)
-    const i64 d = 1 + col;
+    const int d = 1 + col;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const i64 r = R - 1 - u + d;
+      const int r = R - 1 - u + d;
       const bool ok = r < R && r >= d;
       ea[u] = ld_or_zero(src + r * n + e_ch, ok);
       oa[u] = ld_or_zero(src + r * n + o_ch, ok);
     }
-    for (i64 row0 = R - 1; row0 >= 0; row0 -= U) {
+    for (int row0 = R - 1; row0 >= 0; row0 -= U) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const i64 row = row0 - u;
+        const int row = row0 - u;
         if (row >= 0) {
           T v = T(0);
           if (row + d < R) {
@@ -101,7 +106,7 @@ iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i6
           dst[row * n + ch] = v;
           prev = v;
         }
-        const i64 r = row - U + d;
+        const int r = row - U + d;
         const bool ok = r < R && r >= d;
         ea[u] = ld_or_zero(src + r * n + e_ch, ok);
         oa[u] = ld_or_zero(src + r * n + o_ch, ok);
@@ -127,6 +132,7 @@ template <typename T>
 int iadrt_launch(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st) {
   const int L = num_iters(n);
+  if (n > 32768) return ADRT_GB300_ERR_TOO_LARGE;  // 32-bit in-plane offsets
   const i64 planes = batch * 4;
   const i64 elems = planes * n * (2 * n - 1);
   if (L == 0) {
@@ -138,10 +144,17 @@ int iadrt_launch(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   T *bufs[2] = {static_cast<T *>(ws), static_cast<T *>(ws) + elems};
   const T *src = in;
   const i64 threads = planes * n;
-  const unsigned grid = (unsigned)((threads + 127) / 128);
+  // Few chains (small batches): 32-thread blocks so that they spread over
+  // all SMs; otherwise 128.
+  const int bs = threads >= (i64)152 * 4 * 128 ? 128 : 32;
+  const unsigned grid = (unsigned)((threads + bs - 1) / bs);
+  constexpr int U_DEEP = sizeof(T) == 4 ? 32 : 16;
   for (int s = 0; s < L; ++s) {
     T *dst = (s == L - 1) ? out : bufs[s & 1];
-    iadrt_stage_kernel<T><<<grid, 128, 0, st>>>(src, dst, planes, n, s);
+    if (n >= 1024)
+      iadrt_stage_kernel<T, U_DEEP><<<grid, bs, 0, st>>>(src, dst, planes, n, s);
+    else
+      iadrt_stage_kernel<T, U_DEEP / 2><<<grid, bs, 0, st>>>(src, dst, planes, n, s);
     const int rc = launch_status();
     if (rc) return rc;
     src = dst;
