@@ -104,26 +104,26 @@ __global__ void stitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64
 // axes when q is odd; with vc = n-1 the last column comes from column 0 of
 // quadrant q+1 (rows reversed for q = 3).  Reference: src/adrt/utils.py:137-188.
 template <typename W>
-__global__ void unstitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n, i64 vc) {
-  const i64 C = 2 * n - 1, OR = 3 * n - 2;
-  const i64 total = batch * 4 * C * n;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 c = idx % n;
-    const i64 r = (idx / n) % C;
-    const int q = (int)((idx / (n * C)) % 4);
-    const i64 b = idx / (4 * C * n);
-    const i64 rs = (q & 1) ? C - 1 - r : r;
-    const i64 cs = (q & 1) ? n - 1 - c : c;
-    const i64 R = rs + (q >= 2 ? n - 1 : 0);
-    i64 src;
-    if (cs < vc) {
-      src = ((b * OR + R) * 4 + q) * vc + cs;
-    } else {
-      const i64 R2 = q == 3 ? OR - 1 - R : R;
-      src = ((b * OR + R2) * 4 + (q + 1) % 4) * vc;
-    }
-    out[idx] = in[src];
+__global__ void __launch_bounds__(256) unstitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch,
+                                                       i64 n_, i64 vc_) {
+  // One block per output row (b, q, r): per-row index work once, then a
+  // contiguous (or reversed, for odd q) sweep over the row's n columns.
+  const unsigned n = (unsigned)n_, vc = (unsigned)vc_;
+  const unsigned C = 2 * n - 1, OR = 3 * n - 2;
+  const i64 row_id = blockIdx.x;
+  const unsigned r = (unsigned)(row_id % C);
+  const i64 bq = row_id / C;
+  const unsigned q = (unsigned)(bq & 3);
+  const i64 b = bq >> 2;
+  const unsigned rs = (q & 1) ? C - 1 - r : r;
+  const unsigned R = rs + (q >= 2 ? n - 1 : 0);
+  const W *srow = in + ((b * OR + R) * 4 + q) * (i64)vc;
+  const unsigned R2 = q == 3 ? OR - 1 - R : R;
+  const W *sext = in + ((b * OR + R2) * 4 + ((q + 1) & 3)) * (i64)vc;
+  W *orow = out + row_id * (i64)n;
+  for (unsigned c = threadIdx.x; c < n; c += 256) {
+    const unsigned cs = (q & 1) ? n - 1 - c : c;
+    orow[c] = cs < vc ? srow[cs] : sext[0];
   }
 }
 
@@ -243,7 +243,16 @@ int stitch_launch(const void *in, void *out, i64 batch, i64 n, int rr, size_t es
 }
 
 int unstitch_launch(const void *in, void *out, i64 batch, i64 n, i64 vc, size_t es, cudaStream_t st) {
-  BY_SIZE(es, unstitch_kernel, batch * 4 * (2 * n - 1) * n, batch, n, vc)
+  const i64 rows = batch * 4 * (2 * n - 1);
+  if (rows > 0x7fffffffll || n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
+  const unsigned grid = (unsigned)rows;
+  switch (es) {
+    case 1: unstitch_kernel<word<1>::t><<<grid, 256, 0, st>>>((const word<1>::t *)in, (word<1>::t *)out, batch, n, vc); break;
+    case 2: unstitch_kernel<word<2>::t><<<grid, 256, 0, st>>>((const word<2>::t *)in, (word<2>::t *)out, batch, n, vc); break;
+    case 4: unstitch_kernel<word<4>::t><<<grid, 256, 0, st>>>((const word<4>::t *)in, (word<4>::t *)out, batch, n, vc); break;
+    case 8: unstitch_kernel<word<8>::t><<<grid, 256, 0, st>>>((const word<8>::t *)in, (word<8>::t *)out, batch, n, vc); break;
+    default: return ADRT_GB300_ERR_DTYPE;
+  }
   return launch_status();
 }
 

@@ -9,7 +9,7 @@ and as the command line under a profiler.
 
 Ops: adrt, bdrt, iadrt, adjoint, adrt_step, bdrt_step, fmg_restriction,
 fmg_prolongation, fmg_highpass, iadrt_fmg, ragged, cg, pcg, precond,
-net_forward, net_train.
+interp, unstitch, coords, net_forward, net_train.
 """
 
 from __future__ import annotations
@@ -21,7 +21,8 @@ import sys
 import torch
 
 OPS = ("adrt", "bdrt", "iadrt", "adjoint", "adrt_step", "bdrt_step", "fmg_restriction", "fmg_prolongation",
-       "fmg_highpass", "iadrt_fmg", "ragged", "cg", "pcg", "precond", "net_forward", "net_train")
+       "fmg_highpass", "iadrt_fmg", "ragged", "cg", "pcg", "precond", "interp", "unstitch", "coords",
+       "net_forward", "net_train")
 
 
 def _setup(op: str, n: int, batch: int, dtype, dev):
@@ -83,6 +84,24 @@ def _setup(op: str, n: int, batch: int, dtype, dev):
 
         M = precond.ConvPreconditioner(sum(precond.basis(4)))
         return (lambda: M.apply(img)), es * batch * 2 * n * n, batch
+    if op == "interp":
+        from adrt_gb300 import utils
+
+        return (lambda: utils.interp_to_cart(y)), es * batch * (A + 4 * n * n), batch
+    if op == "unstitch":
+        from adrt_gb300 import utils
+
+        s = utils.stitch_adrt(y)
+        return (lambda: utils.unstitch_adrt(s)), es * batch * 2 * A, batch
+    if op == "coords":
+        from adrt_gb300 import utils
+
+        g = torch.Generator(device=dev)
+        g.manual_seed(3)
+        count = batch * n * n
+        theta = (torch.rand(count, generator=g, device=dev, dtype=dtype) - 0.5) * 3.2
+        tt = (torch.rand(count, generator=g, device=dev, dtype=dtype) - 0.5) * 1.4
+        return (lambda: utils.coord_cart_to_adrt(theta, tt, n)), 0, batch
     if op in ("net_forward", "net_train"):
         from adrt_gb300.learned import PreconditionerNet
 
