@@ -93,60 +93,6 @@ __device__ __forceinline__ int sweep_iters(int pos) {
 }
 
 
-// ---- TMA (bulk copy engine) and mbarrier helpers ---------------------------
-
-__device__ __forceinline__ unsigned smem_addr(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
-  unsigned done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-// Global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte
-// aligned) that completes `bytes` transactions on `bar`.
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         unsigned long long *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ unsigned long long now_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Wait for phase `parity` of `bar`, at most about two seconds of wall clock;
-// false if that bound expired.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
-  const unsigned long long t0 = now_ns();
-  while (!mbar_try_wait(bar, parity)) {
-    if (now_ns() - t0 > 2000000000ull) return false;
-  }
-  return true;
-}
-
 // ---------------------------------------------------------------------------
 // Group 1: stages 0 and 1 on one member quad, 4 positions.
 //   m[jj][k]  member jj of the quad, position k
@@ -499,7 +445,6 @@ __device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, i
 // = rows 8b..8b+7), so the 16-byte chunk index is XOR-swizzled with
 // (row >> 3) & 7: the eight lanes of a quarter-warp then hit eight different
 // bank groups when writing, and a row's eight chunks are distinct when read.
-__device__ __forceinline__ int ost_chunk(int row, int c) { return c ^ ((row >> 3) & 7); }
 
 template <int L1>
 __device__ __forceinline__ void group2_passB(const float *xs, float *ost, int c0, int n) {
