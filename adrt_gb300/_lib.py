@@ -81,6 +81,8 @@ SIGNATURES = {
     "adrt_gb300_cg_direction": [_v, _v, _v, _v, _v, _i64, _i64, _int, _v],
     "adrt_gb300_axpy": [ctypes.c_double, _v, _v, _i64, _int, _v],
     "adrt_gb300_precond_conv": [_v, _v, _i64, _i64, ctypes.POINTER(ctypes.c_double), _int, _int, _v],
+    "adrt_gb300_precond_dot_workspace_size": [_i64, _i64],
+    "adrt_gb300_precond_conv_dot": [_v, _v, _i64, _i64, ctypes.POINTER(ctypes.c_double), _int, _int, _v, _v, _sz, _v],
     "adrt_gb300_tune_set": [_int, _int, _i64, _int, _int, _int, _int],
     "adrt_gb300_tune_get": [_int, _int, _i64, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int),
                             ctypes.POINTER(_int)],
@@ -108,6 +110,7 @@ _RESTYPES = {
     "adrt_gb300_status_string": ctypes.c_char_p,
     "adrt_gb300_sumsq_workspace_size": _sz,
     "adrt_gb300_sumsq_batched_workspace_size": _sz,
+    "adrt_gb300_precond_dot_workspace_size": _sz,
     "adrt_gb300_launch_count": ctypes.c_uint64,
     "adrt_gb300_cg_workspace_size": _sz,
 }

@@ -78,6 +78,9 @@ class _State:
             self.p = self.z.clone()
             self.rs = self.dot(self.r, self.z)
             self.rz_new = torch.empty_like(self.rs)
+            self.fused = hasattr(precond, "apply_dot")
+            if self.fused:
+                self.pws = precond.dot_workspace(self.B, n, b.device)
         else:
             self.p = self.r.clone()
             self.rs = self.rr.clone()
@@ -99,6 +102,8 @@ class _State:
             setattr(self, name, getattr(self, name).index_select(0, sel).contiguous())
         self.B = int(sel.numel())
         self.ws = torch.empty(_lib.load().adrt_gb300_cg_workspace_size(self.B), dtype=torch.uint8, device=self.dev)
+        if self.precond is not None and self.fused:
+            self.pws = self.precond.dot_workspace(self.B, self.x.shape[-1], self.dev)
 
     def dot(self, a, b):
         out = torch.empty(self.B, dtype=torch.float64, device=self.dev)
@@ -122,10 +127,13 @@ class _State:
         # Images whose residual reached the tolerance stop here.
         self.active.mul_((self.rs_new > thr2).to(torch.int32))
         if self.precond is not None:
-            self.precond.apply(self.r, out=self.z)
-            rc = lib.adrt_gb300_batched_dot(self.r.data_ptr(), self.z.data_ptr(), self.rz_new.data_ptr(), self.B,
-                                            self.per, self.code, self.ws.data_ptr(), self.stream())
-            _lib.check(rc, "batched_dot")
+            if self.fused:  # z = M r and <r, z> in one kernel
+                self.precond.apply_dot(self.r, self.z, self.rz_new, self.pws)
+            else:
+                self.precond.apply(self.r, out=self.z)
+                rc = lib.adrt_gb300_batched_dot(self.r.data_ptr(), self.z.data_ptr(), self.rz_new.data_ptr(), self.B,
+                                                self.per, self.code, self.ws.data_ptr(), self.stream())
+                _lib.check(rc, "batched_dot")
             d, num = self.z, self.rz_new
         else:
             d, num = self.r, self.rs_new

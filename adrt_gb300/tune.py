@@ -120,8 +120,10 @@ def _synthetic(op, n, dtype, batch, device):
 
 
 def autotune(op: str = "adrt", n: int = 1024, dtype=torch.float32, *, batch: int | None = None, reps: int = 5,
-             apply: bool = True, device="cuda") -> TuneResult:
-    """Times the candidates of (op, n, dtype) and installs the fastest."""
+             apply: bool = True, device="cuda", min_gain: float = 0.01) -> TuneResult:
+    """Times the candidates of (op, n, dtype) and installs the fastest, if it
+    beats the built-in configuration by at least `min_gain` (relative);
+    tune at the batch size the transform will run at."""
     dtype = torch.float32 if _dt(dtype) == _lib.F32 else torch.float64
     es = 4 if dtype == torch.float32 else 8
     if batch is None:
@@ -157,6 +159,11 @@ def autotune(op: str = "adrt", n: int = 1024, dtype=torch.float32, *, batch: int
         set_config(op, n, dtype, previous)
     best, best_ms = min(timings, key=lambda t: t[1])
     default_ms = timings[0][1]
+    # Keep the built-in configuration unless a candidate is clearly faster:
+    # differences within timing noise (or candidates that launch identically
+    # at this batch) must not pick a configuration that is worse elsewhere.
+    if best_ms > (1.0 - min_gain) * default_ms:
+        best, best_ms = timings[0]
     if apply:
         set_config(op, n, dtype, best)
     return TuneResult(op, n, "float32" if es == 4 else "float64", best, best_ms, default_ms, timings)

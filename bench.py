@@ -174,14 +174,15 @@ def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
     }
 
 
-def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=60, pc_h=6):
+def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=60, pc_h=5,
+             pc_tilt=-0.25, pc_samples=32):
     """Batched CG on the normal equations of noisy 256 x 256 ellipse phantoms
     (data b = adrt(x) + N(0, (1e-3 max|b|)^2)): plain CG against the learned
     arms, all with the same stopping rule.
 
     * conv_pcg: preconditioned CG with the learned convolution
       preconditioner (a (2h+1)^2 kernel fit as a least-squares inverse of
-      A^T A on white noise, untimed);
+      A^T A on noise images with spectrum |w|^-0.25, untimed);
     * unet_start: plain CG from the encoder-decoder network's starting image
       (network trained here first on pairs the method generates: phantom ->
       adrt -> noise -> plain CG to 1e-5, untimed);
@@ -253,14 +254,15 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
         })
 
     t0 = time.perf_counter()
-    M = precond.fit(n, h=pc_h, samples=16, seed=0, device=dev)
+    M = precond.fit(n, h=pc_h, samples=pc_samples, seed=0, device=dev, tilt=pc_tilt)
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
     cgmod.cg(b_te[:16], tol=tol, max_iters=200, graph=True, precond=M)  # warm
     pcg, t_pcg = timed(lambda: solve(M=M))
     arm("conv_pcg", finish(pcg), t_pcg)
     lo, hi = M.symbol_range()
-    out["conv_preconditioner"] = {"kernel": f"{2 * pc_h + 1}x{2 * pc_h + 1}", "fit_samples": 16,
+    out["conv_preconditioner"] = {"kernel": f"{2 * pc_h + 1}x{2 * pc_h + 1}", "fit_samples": pc_samples,
+                                  "fit_noise_spectrum": f"|w|^{pc_tilt}",
                                   "fit_seconds": t_fit, "symbol_min": lo, "symbol_max": hi}
 
     t0 = time.perf_counter()
@@ -472,7 +474,7 @@ def main():
     if not args.no_tune:
         from adrt_gb300 import tune
 
-        r = tune.autotune("adrt", n, torch.float32, batch=min(B, 32), reps=5, device=dev)
+        r = tune.autotune("adrt", n, torch.float32, batch=B, reps=3, device=dev)
         tuned = {"config": {"width": r.best.width, "max_fused": r.best.max_fused, "chunk_mb": r.best.chunk_mb,
                             "use_fast": r.best.use_fast},
                  "best_ms": r.best_ms, "default_ms": r.default_ms, "candidates": len(r.timings),

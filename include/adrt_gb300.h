@@ -309,6 +309,15 @@ int adrt_gb300_axpy(double alpha, const void *x, void *y, int64_t count, int dty
 int adrt_gb300_precond_conv(const void *x, void *y, int64_t batch, int64_t n, const double *weights, int h,
                             int dtype, void *stream);
 
+/* The same convolution y = K * x, fused with the per-image dot product
+ * dot[i] = <x_i, y_i> (float64, device double[batch]; per-thread partial sums
+ * in the data type, fixed-order float64 combination): preconditioned CG's
+ * <r, M r>.  workspace: adrt_gb300_precond_dot_workspace_size(batch, n)
+ * bytes of device memory. */
+size_t adrt_gb300_precond_dot_workspace_size(int64_t batch, int64_t n);
+int adrt_gb300_precond_conv_dot(const void *x, void *y, int64_t batch, int64_t n, const double *weights, int h,
+                                int dtype, double *dot, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

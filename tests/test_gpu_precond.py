@@ -107,3 +107,17 @@ def test_pcg_compaction_and_graph_identical():
     comp = cgmod.cg(b, tol=1e-5, max_iters=400, compact=0.9, check_every=1, graph=True, precond=M)
     assert torch.equal(full.iterations, comp.iterations)
     assert torch.equal(full.x, comp.x)
+
+
+@pytest.mark.parametrize("n", [5, 64, 100])
+def test_fused_dot_matches_separate(n):
+    M = precond.ConvPreconditioner(_sym_kernel(3, 2))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    x = torch.randn((3, n, n), generator=g, device="cuda")
+    out = torch.empty_like(x)
+    dot = torch.empty(3, dtype=torch.float64, device="cuda")
+    M.apply_dot(x, out, dot, M.dot_workspace(3, n, x.device))
+    assert torch.equal(out, M.apply(x))
+    want = (x.double() * out.double()).sum(dim=(1, 2))
+    assert torch.allclose(dot, want, rtol=1e-5, atol=1e-6)

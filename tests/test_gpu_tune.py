@@ -25,7 +25,9 @@ def clean_table():
 def test_autotune_installs_fastest(op, n, dtype):
     r = tune.autotune(op, n, dtype, batch=4, reps=2)
     assert len(r.timings) == len(tune.candidates(op, n, dtype))
-    assert r.best_ms == min(ms for _, ms in r.timings)
+    fastest = min(ms for _, ms in r.timings)
+    # the fastest candidate, or the built-in one when nothing beats it by 1 %
+    assert r.best_ms == fastest or (r.best == r.timings[0][0] and fastest > 0.99 * r.timings[0][1])
     assert tune.get(op, n, dtype) == r.best
 
 
