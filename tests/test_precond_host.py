@@ -45,3 +45,28 @@ def test_abi_argument_checks():
     assert lib.adrt_gb300_precond_conv(fake, fake, 0, 8, w, 1, _lib.F32, None) == _lib.ERR_SHAPE
     assert lib.adrt_gb300_precond_conv(fake, fake, 1, 8, w, 8, _lib.F32, None) == _lib.ERR_SHAPE
     assert lib.adrt_gb300_precond_conv(fake, fake, 1, 65536, w, 1, _lib.F32, None) == _lib.ERR_TOO_LARGE
+
+
+def test_fused_dot_abi_argument_checks():
+    lib = _lib.load()
+    fake = ctypes.c_void_p(16)
+    w = (ctypes.c_double * 9)()
+    ws = lib.adrt_gb300_precond_dot_workspace_size(4, 64)
+    assert ws == 8 * 4 * 2 * 2
+    assert lib.adrt_gb300_precond_dot_workspace_size(0, 64) == 0
+    assert lib.adrt_gb300_precond_conv_dot(fake, fake, 4, 64, w, 1, _lib.F32, None, fake, ws, None) == _lib.ERR_NULL
+    assert lib.adrt_gb300_precond_conv_dot(fake, fake, 4, 64, w, 1, _lib.F32, fake, None, ws, None) == _lib.ERR_NULL
+    assert lib.adrt_gb300_precond_conv_dot(fake, fake, 4, 64, w, 1, _lib.F32, fake, fake, ws - 1, None) == \
+        _lib.ERR_WORKSPACE
+    assert lib.adrt_gb300_precond_conv_dot(fake, fake, 4, 64, w, 9, _lib.F32, fake, fake, ws, None) == _lib.ERR_SHAPE
+
+
+def test_sumsq_batched_abi_argument_checks():
+    lib = _lib.load()
+    fake = ctypes.c_void_p(16)
+    assert lib.adrt_gb300_sumsq_batched_workspace_size(3) == 3 * lib.adrt_gb300_sumsq_workspace_size()
+    assert lib.adrt_gb300_sumsq_batched_workspace_size(0) == 0
+    assert lib.adrt_gb300_sumsq_batched(None, 2, 16, _lib.F32, fake, fake, None) == _lib.ERR_NULL
+    assert lib.adrt_gb300_sumsq_batched(fake, 0, 16, _lib.F32, fake, fake, None) == _lib.ERR_SHAPE
+    assert lib.adrt_gb300_sumsq_batched(fake, 2, 16, 7, fake, fake, None) == _lib.ERR_DTYPE
+    assert lib.adrt_gb300_sumsq_batched(fake, 70000, 16, _lib.F32, fake, fake, None) == _lib.ERR_TOO_LARGE
