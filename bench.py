@@ -17,6 +17,7 @@ time is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -478,7 +479,7 @@ def main():
         tuned = {"config": {"width": r.best.width, "max_fused": r.best.max_fused, "chunk_mb": r.best.chunk_mb,
                             "use_fast": r.best.use_fast},
                  "best_ms": r.best_ms, "default_ms": r.default_ms, "candidates": len(r.timings),
-                 "batch": min(B, 32)}
+                 "batch": B, "min_gain": 0.01}
     x = mixed_batch(B, n, seed=1000 * rank, device=dev, dtype=torch.float32)
     torch.cuda.synchronize()
 
@@ -493,6 +494,11 @@ def main():
         time.sleep(0.3)
     stream = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # Python's cyclic garbage collector stays off inside the timed regions
+    # (as timeit does): a full collection of this process's objects is a
+    # pause of the interpreter, not of the transform.
+    gc.collect()
+    gc.disable()
     barrier()
     torch.cuda.synchronize()
     launches0 = _lib.launch_count()
@@ -502,6 +508,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     launches = _lib.launch_count() - launches0
+    gc.enable()
     barrier()
     clocks = sampler.stop() if sampler else None
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
@@ -528,6 +535,8 @@ def main():
             warm_ms.append(round(dt * 1e3, 1))
             if i >= 3 and max(warm_ms[-3:]) <= 1.1 * min(warm_ms[-3:]):
                 break
+        gc.collect()
+        gc.disable()
         barrier()
         torch.cuda.synchronize()
         call_ms = []
@@ -538,6 +547,7 @@ def main():
             torch.cuda.synchronize()
             call_ms.append(round((time.perf_counter() - tc) * 1e3, 1))
         t_e2e = max_over_ranks(time.perf_counter() - t0)
+        gc.enable()
         e2e = {
             "value": world * B * args.e2e_steps / t_e2e,
             "unit": UNIT,
