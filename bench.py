@@ -203,11 +203,16 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
     from adrt_gb300 import learned, precond
 
     def timed(fn):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = fn()
-        torch.cuda.synchronize()
-        return r, time.perf_counter() - t0
+        gc.collect()
+        gc.disable()  # no interpreter collection pause inside the timed solve
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            torch.cuda.synchronize()
+            return r, time.perf_counter() - t0
+        finally:
+            gc.enable()
 
     b_te, _ = learned.training_pairs(n_test, n, seed=900_000, tol=1e-5, device=dev)
 
@@ -309,12 +314,17 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
 
     def timed(fn, reps):
         fn()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            r = fn()
-        torch.cuda.synchronize()
-        return r, (time.perf_counter() - t0) / reps
+        gc.collect()
+        gc.disable()  # no interpreter collection pause inside the timed region
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                r = fn()
+            torch.cuda.synchronize()
+            return r, (time.perf_counter() - t0) / reps
+        finally:
+            gc.enable()
 
     ys, t_fwd = timed(lambda: adrt_ragged(imgs), 3)
     inv, t_inv = timed(lambda: iadrt_ragged(ys), 3)
