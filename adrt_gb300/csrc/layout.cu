@@ -77,26 +77,27 @@ __device__ __forceinline__ void truncate_body(const W *__restrict__ in, W *__res
 // odd, last column dropped when remove_repeated, rows offset by n-1 for k >= 2.
 // Reference: src/adrt/utils.py:111-134.
 template <typename W>
-__global__ void stitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch, i64 n,
-                              int remove_repeated) {
-  const i64 C = 2 * n - 1, OR = 3 * n - 2;
-  const i64 vc = n - (remove_repeated ? 1 : 0);
-  const i64 total = batch * OR * 4 * vc;
-  for (i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x; idx < total;
-       idx += (i64)gridDim.x * blockDim.x) {
-    const i64 col = idx % vc;
-    const int k = (int)((idx / vc) % 4);
-    const i64 row = (idx / (4 * vc)) % OR;
-    const i64 b = idx / (4 * vc * OR);
-    const i64 rr = row - (k >= 2 ? n - 1 : 0);
-    W v = W(0);
-    if (rr >= 0 && rr < C) {
-      const i64 sr = (k & 1) ? C - 1 - rr : rr;
-      const i64 sc = (k & 1) ? n - 1 - col : col;
-      v = in[((b * 4 + k) * C + sr) * n + sc];
-    }
-    out[idx] = v;
+__global__ void __launch_bounds__(256) stitch_kernel(const W *__restrict__ in, W *__restrict__ out, i64 batch,
+                                                     i64 n_, int remove_repeated) {
+  // One block per output segment (b, row, k): vc contiguous outputs, read
+  // from one input row (reversed for odd k), or zeros outside quadrant k.
+  const unsigned n = (unsigned)n_;
+  const unsigned C = 2 * n - 1, OR = 3 * n - 2;
+  const unsigned vc = n - (remove_repeated ? 1 : 0);
+  const i64 seg = blockIdx.x;
+  const unsigned k = (unsigned)(seg & 3);
+  const i64 brow = seg >> 2;
+  const unsigned row = (unsigned)(brow % OR);
+  const i64 b = brow / OR;
+  W *o = out + seg * (i64)vc;
+  const int rr = (int)row - (k >= 2 ? (int)n - 1 : 0);
+  if (rr < 0 || rr >= (int)C) {
+    for (unsigned c = threadIdx.x; c < vc; c += 256) o[c] = W(0);
+    return;
   }
+  const unsigned sr = (k & 1) ? C - 1 - (unsigned)rr : (unsigned)rr;
+  const W *irow = in + ((b * 4 + k) * C + sr) * (i64)n;
+  for (unsigned c = threadIdx.x; c < vc; c += 256) o[c] = irow[(k & 1) ? n - 1 - c : c];
 }
 
 // (3n-2, 4, vc) -> (4, 2n-1, n), the inverse of stitch_kernel: quadrant q
@@ -238,7 +239,17 @@ int truncate_launch(const void *in, void *out, i64 batch, i64 n, size_t es, cuda
 }
 
 int stitch_launch(const void *in, void *out, i64 batch, i64 n, int rr, size_t es, cudaStream_t st) {
-  BY_SIZE(es, stitch_kernel, batch * (3 * n - 2) * 4 * n, batch, n, rr)
+  const i64 segs = batch * (3 * n - 2) * 4;
+  if (segs > 0x7fffffffll || n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
+  const unsigned grid = (unsigned)segs;
+  switch (es) {
+    case 1: stitch_kernel<word<1>::t><<<grid, 256, 0, st>>>((const word<1>::t *)in, (word<1>::t *)out, batch, n, rr); break;
+    case 2: stitch_kernel<word<2>::t><<<grid, 256, 0, st>>>((const word<2>::t *)in, (word<2>::t *)out, batch, n, rr); break;
+    case 4: stitch_kernel<word<4>::t><<<grid, 256, 0, st>>>((const word<4>::t *)in, (word<4>::t *)out, batch, n, rr); break;
+    case 8: stitch_kernel<word<8>::t><<<grid, 256, 0, st>>>((const word<8>::t *)in, (word<8>::t *)out, batch, n, rr); break;
+    case 16: stitch_kernel<word<16>::t><<<grid, 256, 0, st>>>((const word<16>::t *)in, (word<16>::t *)out, batch, n, rr); break;
+    default: return ADRT_GB300_ERR_DTYPE;
+  }
   return launch_status();
 }
 
@@ -251,6 +262,7 @@ int unstitch_launch(const void *in, void *out, i64 batch, i64 n, i64 vc, size_t 
     case 2: unstitch_kernel<word<2>::t><<<grid, 256, 0, st>>>((const word<2>::t *)in, (word<2>::t *)out, batch, n, vc); break;
     case 4: unstitch_kernel<word<4>::t><<<grid, 256, 0, st>>>((const word<4>::t *)in, (word<4>::t *)out, batch, n, vc); break;
     case 8: unstitch_kernel<word<8>::t><<<grid, 256, 0, st>>>((const word<8>::t *)in, (word<8>::t *)out, batch, n, vc); break;
+    case 16: unstitch_kernel<word<16>::t><<<grid, 256, 0, st>>>((const word<16>::t *)in, (word<16>::t *)out, batch, n, vc); break;
     default: return ADRT_GB300_ERR_DTYPE;
   }
   return launch_status();
