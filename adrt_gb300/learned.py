@@ -5,8 +5,10 @@ kernels, ReLU, 2 x 2 average pooling down, nearest 2x upsampling up, skip
 connections added before the decoder's first activation) maps the scaled
 back-projection u = s * A^T b of the data to an image x0; CG then starts from
 x0 instead of 0.  The reference has no learned component: its reconstruction
-is CG from zero (docs/examples.cginverse.md:40-67), which stays the fallback
-and the judge of every solve (a solve counts when CG reaches the tolerance).
+is CG from zero (docs/examples.cginverse.md:40-67), which stays the fallback;
+every solve uses CG's own stopping rule (a solve counts when CG reaches the
+tolerance).  The learned convolution preconditioner of
+adrt_gb300.precond is the other learned component.
 
 Everything runs in the library's kernels (include/adrt_gb300_net.h): the
 3 x 3 convolutions with 32..256 channels on the tcgen05 tensor cores (bf16
