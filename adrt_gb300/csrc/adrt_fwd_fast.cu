@@ -580,7 +580,7 @@ bool fast_forward_eligible(i64 n, size_t elem) { return elem == 4 && n >= 64 && 
 // faster than chunks whose intermediate stays in L2 (n = 1024, 256 images:
 // 52.1k img/s with one launch pair, 46.9k with 5-image chunks): the launch
 // tails cost more than the intermediate's round trip through HBM, which has
-// bandwidth to spare here.  Built-in budget 4 GB of intermediate (236 images
+// bandwidth to spare here.  Built-in budget 4 GB of intermediate (248 images
 // at n = 1024), or the tuned one; chunks are balanced so the last one is not
 // a small tail.
 static i64 fast_chunk(i64 batch, i64 n) {

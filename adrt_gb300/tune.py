@@ -157,16 +157,23 @@ def autotune(op: str = "adrt", n: int = 1024, dtype=torch.float32, *, batch: int
             timings.append((cfg, ms[len(ms) // 2]))
     finally:
         set_config(op, n, dtype, previous)
-    best, best_ms = min(timings, key=lambda t: t[1])
+    best, best_ms = select(timings, min_gain)
     default_ms = timings[0][1]
-    # Keep the built-in configuration unless a candidate is clearly faster:
-    # differences within timing noise (or candidates that launch identically
-    # at this batch) must not pick a configuration that is worse elsewhere.
-    if best_ms > (1.0 - min_gain) * default_ms:
-        best, best_ms = timings[0]
     if apply:
         set_config(op, n, dtype, best)
     return TuneResult(op, n, "float32" if es == 4 else "float64", best, best_ms, default_ms, timings)
+
+
+def select(timings, min_gain: float = 0.01):
+    """(config, ms) to install from [(config, ms), ...] whose first entry is
+    the built-in configuration: the fastest candidate, unless it beats the
+    built-in one by less than `min_gain` (relative) -- differences within
+    timing noise, or candidates that launch identically at the tuning batch,
+    must not pick a configuration that is worse elsewhere."""
+    best, best_ms = min(timings, key=lambda t: t[1])
+    if best_ms > (1.0 - min_gain) * timings[0][1]:
+        return timings[0]
+    return best, best_ms
 
 
 def _default_path():

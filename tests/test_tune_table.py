@@ -55,3 +55,25 @@ def test_workspace_follows_table(tune):
     tune.set_config("adrt", 1024, "float64", tune.Config(max_fused=3))
     w1 = _lib.workspace_size(_lib.OP_ADRT, 1, 1024, _lib.F64)
     assert w1 == 2 * w0
+
+
+def test_select_keeps_builtin_within_noise():
+    from adrt_gb300.tune import Config, select
+
+    base, a, b = Config(), Config(128, 0, 0, -1), Config(256, 3, 96, 0)
+    assert select([(base, 1.00), (a, 0.995), (b, 1.2)]) == (base, 1.00)      # 0.5 % faster: noise
+    assert select([(base, 1.00), (a, 0.98), (b, 0.95)]) == (b, 0.95)        # clearly faster
+    assert select([(base, 1.00), (a, 0.98)], min_gain=0.05) == (base, 1.00)
+    assert select([(base, 1.00)]) == (base, 1.00)
+
+
+def test_fast_forward_chunks_are_balanced():
+    from adrt_gb300 import _lib
+
+    lib_ws = lambda b: _lib.workspace_size(_lib.OP_ADRT, b, 1024, _lib.F32)  # noqa: E731
+    per = 4 * 32 * 32 * 1056 * 4  # one image's intermediate at n = 1024
+    assert lib_ws(8) == 8 * per                   # small batches: one chunk
+    assert lib_ws(248) == 248 * per               # 4 GiB budget: 248 images
+    assert lib_ws(249) == 125 * per               # two balanced chunks (125 + 124), not 248 + 1
+    assert lib_ws(256) == 128 * per
+    assert lib_ws(1000) == 200 * per              # five chunks of 200
