@@ -116,17 +116,18 @@ int table_for(long long n, InterpTable *t) {
 
 }  // namespace
 
-// out[b][o][a] = factor[a] * in[b][idx[o][a]] (or 0 where idx < 0).
+// out[b][o][a] = factor[a] * in[b][idx[o][a]] (or 0 where idx < 0).  Grid:
+// x over one image's 4 n^2 outputs (32-bit indices), y over images; the
+// angle index a = k mod 4n is a mask (4n is a power of two).
 template <typename T>
 __global__ void interp_kernel(const T *__restrict__ in, T *__restrict__ out, const int *__restrict__ idx,
-                              const T *__restrict__ fac, long long batch, long long n) {
-  const long long per_out = 4 * n * n, per_in = 4 * (2 * n - 1) * n;
-  const long long total = batch * per_out;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long b = i / per_out, k = i % per_out;
-    const int src = __ldg(idx + k);
-    out[i] = src >= 0 ? mul_rn(__ldg(fac + k % (4 * n)), in[b * per_in + src]) : T(0);
+                              const T *__restrict__ fac, unsigned n) {
+  const unsigned per_out = 4 * n * n, per_in = 4 * (2 * n - 1) * n, amask = 4 * n - 1;
+  const T *src = in + (size_t)blockIdx.y * per_in;
+  T *dst = out + (size_t)blockIdx.y * per_out;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < per_out; k += gridDim.x * blockDim.x) {
+    const int s = __ldg(idx + k);
+    dst[k] = s >= 0 ? mul_rn(__ldg(fac + (k & amask)), src[s]) : T(0);
   }
 }
 
@@ -134,16 +135,25 @@ int interp_to_cart_launch(const void *in, void *out, long long batch, long long 
   InterpTable tab;
   int rc = table_for(n, &tab);
   if (rc) return rc;
-  long long blocks = (batch * 4 * n * n + 255) / 256;
-  if (blocks > 152 * 64) blocks = 152 * 64;
-  if (dtype == ADRT_GB300_F32)
-    interp_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float *>(in),
-                                                           static_cast<float *>(out), tab.idx, tab.fac32, batch, n);
-  else
-    interp_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(static_cast<const double *>(in),
-                                                            static_cast<double *>(out), tab.idx, tab.fac64, batch,
-                                                            n);
-  return launch_status();
+  const long long per_out = 4 * n * n;
+  long long bx = (per_out + 255) / 256;
+  if (bx > 2048) bx = 2048;
+  const size_t es = dtype == ADRT_GB300_F32 ? 4 : 8;
+  for (long long b0 = 0; b0 < batch; b0 += 65535) {
+    const unsigned nb = (unsigned)(batch - b0 < 65535 ? batch - b0 : 65535);
+    const dim3 grid((unsigned)bx, nb);
+    const char *ib = static_cast<const char *>(in) + (size_t)b0 * 4 * (2 * n - 1) * n * es;
+    char *ob = static_cast<char *>(out) + (size_t)b0 * per_out * es;
+    if (dtype == ADRT_GB300_F32)
+      interp_kernel<float><<<grid, 256, 0, st>>>(reinterpret_cast<const float *>(ib), reinterpret_cast<float *>(ob),
+                                                 tab.idx, tab.fac32, (unsigned)n);
+    else
+      interp_kernel<double><<<grid, 256, 0, st>>>(reinterpret_cast<const double *>(ib),
+                                                  reinterpret_cast<double *>(ob), tab.idx, tab.fac64, (unsigned)n);
+    rc = launch_status();
+    if (rc) return rc;
+  }
+  return ADRT_GB300_OK;
 }
 
 }  // namespace adrtg
