@@ -11,11 +11,9 @@ There is no CPU compute path.
 from __future__ import annotations
 
 import collections.abc
-import itertools
 import math
 import typing
 
-import numpy as np
 import torch
 
 from . import core, utils
@@ -91,8 +89,9 @@ def iadrt_fmg_batched(a, /, *, max_iters: int | None = None):
 def iadrt_fmg(a, /, *, max_iters: int | None = None):
     """Approximate inverse of the ADRT by the full multigrid method, refined
     until the residual norm stops decreasing or `max_iters` estimates were made.
-    No batch dimension.  Reference: src/adrt/__init__.py:69-148 (same iteration
-    and stopping rule; the residual norm is accumulated in float64)."""
+    No batch dimension.  Reference: src/adrt/__init__.py:69-148 (the same
+    estimates and stopping rule: keep an estimate while each new one has a
+    strictly smaller residual norm; the norm is accumulated in float64)."""
     if a.ndim > 3:
         raise ValueError(f"batch dimension not supported for iadrt_fmg, got {a.ndim} dimensions")
     if max_iters is not None and max_iters < 1:
@@ -101,16 +100,15 @@ def iadrt_fmg(a, /, *, max_iters: int | None = None):
     t = st.t
     ws = torch.empty(_lib.load().adrt_gb300_sumsq_workspace_size(), dtype=torch.uint8, device=st.device)
     acc = torch.empty((), dtype=torch.float64, device=st.device)
-    inv1 = t
-    for (inv1, res1), (_, res2) in itertools.pairwise(
-        itertools.chain(
-            (
-                (x, _residual_norm(x, t, ws, acc))
-                for x in itertools.islice(core.iadrt_fmg_iter(t, copy=False), max_iters)
-            ),
-            [(t, np.inf)],
-        )
-    ):
-        if not res2 < res1:
+    estimates = core.iadrt_fmg_iter(t, copy=False)
+    kept = next(estimates)
+    kept_norm = _residual_norm(kept, t, ws, acc)
+    made = 1
+    while max_iters is None or made < max_iters:
+        cand = next(estimates)
+        made += 1
+        cand_norm = _residual_norm(cand, t, ws, acc)
+        if not cand_norm < kept_norm:  # no decrease, or a NaN norm: stop at the kept one
             break
-    return st.finish(inv1.clone())
+        kept, kept_norm = cand, cand_norm
+    return st.finish(kept.clone())

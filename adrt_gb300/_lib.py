@@ -46,6 +46,7 @@ SIGNATURES = {
     "adrt_gb300_num_iters": [_i64],
     "adrt_gb300_launch_count": [],
     "adrt_gb300_device_status": [_v],
+    "adrt_gb300_probe_dadd": [_v, _int, _int, _int, _v],
     "adrt_gb300_workspace_size": [_int, _i64, _i64, _int, ctypes.POINTER(_sz)],
     "adrt_gb300_adrt": [_v, _v, _i64, _i64, _int, _v, _sz, _v],
     "adrt_gb300_adrt_noalloc": [_v, _v, _i64, _i64, _int, _v],

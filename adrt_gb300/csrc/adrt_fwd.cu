@@ -231,11 +231,8 @@ static int launch_fwd_pass_w(const FwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S;
   const size_t smem = 2 * sizeof(T) * FwdTile<T, ROWS, W>::BUF;
   auto kern = fwd_pass_kernel<T, S, FIRST, LAST, W>;
-  static bool configured = false;  // per-instantiation, host-side only
-  if (!configured) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};  // per instantiation: devices done
+  if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
   const i64 tiles = a.batch * fwd_pass_tiles(a.n, S, W);
   kern<<<(unsigned)tiles, fwd_threads<T, S>(), smem, st>>>(a);
   return launch_status();
@@ -551,11 +548,8 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
   // The copies above are from pageable memory: they complete before the calls return.
   constexpr size_t smem = 2 * sizeof(T) * FwdTile<T, 32, kFwdWNarrow>::BUF;
   auto kern = ragged_fwd_kernel<T>;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -623,12 +623,9 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
   if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
   unsigned *err = fast_error_word();
   if (!err) return ADRT_GB300_ERR_CUDA;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(fast::pass_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
-    cudaFuncSetAttribute(fast::pass_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fast::SMEM);
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured_a{0}, configured_b{0};
+  if (const int rc = smem_limit_once((const void *)fast::pass_a_kernel, fast::SMEM, configured_a)) return rc;
+  if (const int rc = smem_limit_once((const void *)fast::pass_b_kernel, fast::SMEM, configured_b)) return rc;
   i64 chunk = fast_chunk(batch, n);
   if ((i64)ws_bytes < per * chunk) chunk = (i64)ws_bytes / per;
   float *inter = static_cast<float *>(ws);

@@ -205,11 +205,8 @@ static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
   constexpr int ROWS = 1 << S, NT = bwd_threads<S>();
   const size_t smem = 2 * sizeof(T) * BwdTile<T, ROWS, NT>::BUF;
   auto kern = bwd_pass_kernel<T, S, FIRST, LAST>;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
   const i64 A_lo = i64(1) << a.k0;
   const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W);
   const i64 tiles = a.batch * 4 * ((a.n >> a.k0) >> S) * A_lo * col_tiles;

@@ -6,6 +6,7 @@
 // without fast-math; adds that must not be reordered use __fadd_rn/__dadd_rn.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -63,6 +64,21 @@ inline int launch_status() {
   count_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ADRT_GB300_OK : ADRT_GB300_ERR_CUDA;
+}
+
+// Raises a kernel's dynamic shared-memory limit on the current device.  The
+// attribute belongs to the device, so it is set once per device: `done` is
+// that kernel's bitmask of devices (0..63) already configured.  Two host
+// threads may both set it the first time; setting it twice is harmless.
+inline int smem_limit_once(const void *kern, size_t smem, std::atomic<unsigned long long> &done) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ADRT_GB300_ERR_CUDA;
+  const unsigned long long bit = 1ull << dev;
+  if (done.load(std::memory_order_acquire) & bit) return ADRT_GB300_OK;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return ADRT_GB300_ERR_CUDA;
+  done.fetch_or(bit, std::memory_order_acq_rel);
+  return ADRT_GB300_OK;
 }
 
 }  // namespace adrtg

@@ -82,19 +82,31 @@ void compute_table(long long n, int *idx, float *f32, double *f64) {
   }
 }
 
+// Builds the selection table on the host and uploads it.  The table is kept
+// per (device, n) until the process exits (4 n^2 ints: 4 MiB at n = 1024).
+// The upload is a synchronous copy, so the first call for each n on a device
+// must come before any stream capture.  On failure nothing stays allocated.
 int build_table(long long n, InterpTable *out) {
   std::vector<int> idx((size_t)(4 * n * n));
   std::vector<float> f32((size_t)(4 * n));
   std::vector<double> f64((size_t)(4 * n));
   compute_table(n, idx.data(), f32.data(), f64.data());
-  if (cudaMalloc(&out->idx, sizeof(int) * idx.size()) != cudaSuccess ||
-      cudaMalloc(&out->fac32, sizeof(float) * f32.size()) != cudaSuccess ||
-      cudaMalloc(&out->fac64, sizeof(double) * f64.size()) != cudaSuccess)
+  InterpTable t{};
+  const bool ok =
+      cudaMalloc(&t.idx, sizeof(int) * idx.size()) == cudaSuccess &&
+      cudaMalloc(&t.fac32, sizeof(float) * f32.size()) == cudaSuccess &&
+      cudaMalloc(&t.fac64, sizeof(double) * f64.size()) == cudaSuccess &&
+      cudaMemcpy(t.idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+      cudaMemcpy(t.fac32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+      cudaMemcpy(t.fac64, f64.data(), sizeof(double) * f64.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    // cudaFree(nullptr) is a no-op, so a partial allocation is released whole.
+    cudaFree(t.idx);
+    cudaFree(t.fac32);
+    cudaFree(t.fac64);
     return ADRT_GB300_ERR_CUDA;
-  if (cudaMemcpy(out->idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(out->fac32, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(out->fac64, f64.data(), sizeof(double) * f64.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-    return ADRT_GB300_ERR_CUDA;
+  }
+  *out = t;
   return ADRT_GB300_OK;
 }
 

@@ -15,6 +15,12 @@
 // reads, so nothing needs clearing between calls.  Calls that overlap on the
 // GPU (different streams, or host threads racing) use the same scratch and
 // race; callers must order them.
+//
+// Set-up: the first call on each device looks up the scratch array's device
+// address (cudaGetSymbolAddress, with that device current) and caches it, so
+// that first call should come before any stream capture.  The cached address
+// belongs to the device's primary context: a process that calls
+// cudaDeviceReset must not use this entry point on that device afterwards.
 #include <mutex>
 
 #include "common.cuh"
@@ -63,7 +69,8 @@ extern "C" int adrt_gb300_adrt_noalloc(const void *in, void *out, int64_t batch,
   if (batch < 1 || n < 1 || !is_pow2(n)) return ADRT_GB300_ERR_SHAPE;
   if (n > (i64(1) << 24)) return ADRT_GB300_ERR_TOO_LARGE;
   const size_t es = dtype_size(dtype);
-  // One image's intermediate must fit; larger batches run one image at a time.
+  // One image's intermediate must fit; a batch runs in chunks of as many
+  // images as fit in the scratch (at least one).
   if (fwd_workspace_bytes(1, n, es) > kScratchBytes) return ADRT_GB300_ERR_TOO_LARGE;
   void *scratch = nullptr;
   const int rc = scratch_address(&scratch);

@@ -40,6 +40,56 @@ def bytes_per_image(n: int, elem: int) -> int:
     return elem * (n * n + 4 * n * (2 * n - 1))
 
 
+def bytes_per_image_bdrt(n: int, elem: int) -> int:
+    """Compulsory traffic of bdrt / iadrt, per direction: one (4, 2n-1, n)
+    array (read once; the output, written once, is the same size)."""
+    return elem * 4 * n * (2 * n - 1)
+
+
+def min_adds_per_image(n: int) -> int:
+    """Adds a forward ADRT cannot avoid: per quadrant and stage, an output
+    (row group, angle a, offset c) needs an add only where both operands can
+    be non-zero, c in [ceil(a/2), n + floor(a/2)) -- n - (a mod 2) offsets;
+    summed over the stage's rows and angles that is n^2 - n/2 per stage."""
+    L = max(0, (n - 1).bit_length())
+    return 4 * L * (n * n - n // 2)
+
+
+def dadd_rate(torch, dev, lib_mod, iters: int = 4096) -> float:
+    """The GPU's float64 add rate (adds/s), measured with the library's probe
+    kernel: best of 3 timed launches after one warm-up."""
+    blocks, threads = 152 * 8, 256
+    out = torch.empty(blocks * threads, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream(dev)
+    lib = lib_mod.load()
+    best = None
+    for i in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        lib_mod.check(lib.adrt_gb300_probe_dadd(out.data_ptr(), blocks, threads, iters, st.cuda_stream), "probe_dadd")
+        b.record(st)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1000.0
+        if i and (best is None or t < best):
+            best = t
+    return blocks * threads * 8.0 * iters / best
+
+
+def sample_parity(x, y) -> dict:
+    """Bit-for-bit comparison of the GPU's results for the sampled images of
+    the timed batch with the reference package's adrt of the same images."""
+    import numpy as np
+
+    from oracle import ref
+
+    A = ref.load()
+    if A is None:
+        return {"reference": "not installed on this host"}
+    want = A.adrt(x)
+    same = bool(np.array_equal(want.view(np.uint32), y.view(np.uint32)))
+    return {"images": int(x.shape[0]), "bit_exact": same, "checker": "reference package adrt.adrt"}
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -140,65 +190,135 @@ def gpu_uuid(torch, dev) -> str:
         return str(dev)
 
 
-def cpu_baseline_run(n: int, dtype: str, budget_s: float, batch: int = 8):
-    """Times the CPU restatement (all host threads) on a bounded sample."""
-    import numpy as np
-
-    from oracle import oracle
-
-    kind = "port"
-    fn = oracle.adrt
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine)."""
     try:
-        from oracle import ref
-
-        A = ref.load()
-        if A is not None:
-            fn, kind = A.adrt, "reference"
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                return line.split(":", 1)[1].strip()
     except Exception:
         pass
-    x = np.random.default_rng(0).random((batch, n, n), dtype=np.float32).astype(dtype)
-    fn(x[:1])  # warm
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.machine()
+
+
+class _OpenMP:
+    """Thread control for the reference's OpenMP runtime (libgomp, loaded by
+    its extension): the reference exposes none, so the runtime's own
+    omp_set_num_threads is called; it applies to parallel regions that this
+    (the calling) thread starts next."""
+
+    def __init__(self):
+        import ctypes
+
+        try:
+            self.lib = ctypes.CDLL("libgomp.so.1")
+        except OSError:
+            self.lib = None
+
+    def max_threads(self) -> int:
+        return int(self.lib.omp_get_max_threads()) if self.lib else 1
+
+    def set_threads(self, k: int) -> None:
+        if self.lib:
+            self.lib.omp_set_num_threads(int(k))
+
+
+def cpu_sample(n: int, per_half: int = 4):
+    """A bounded sample of the benchmark workload on the host: `per_half`
+    uniform [0, 1) images and `per_half` ellipse phantoms of n x n float32
+    (the batch's two halves, same generators, generated on the CPU)."""
+    import importlib.util
+
+    # The data module alone (pure NumPy/torch), not the adrt_gb300 package:
+    # the reference arm loads nothing of this library.
+    spec = importlib.util.spec_from_file_location("_bench_data", os.path.join(ROOT, "adrt_gb300", "data.py"))
+    data = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(data)
+    return data.mixed_batch(2 * per_half, n, seed=0, device="cpu").numpy()
+
+
+def time_cpu(fn, x, steps: int, warmup: int, budget_s: float | None = None):
+    """Images/s of fn over the batch x: `warmup` untimed calls, then `steps`
+    timed calls (or, with a budget, calls until `budget_s` has elapsed)."""
+    for _ in range(warmup):
+        fn(x)
     t0 = time.perf_counter()
-    imgs = 0
+    calls = 0
     while True:
         fn(x)
-        imgs += batch
+        calls += 1
         el = time.perf_counter() - t0
-        if el >= budget_s:
+        if (budget_s is None and calls >= steps) or (budget_s is not None and el >= budget_s):
             break
-    return {
-        "value": imgs / el,
-        "unit": UNIT,
-        "cores": oracle.threads(),
-        "kind": kind,
-        "sample": f"{imgs} images of {n}x{n} {dtype} in batches of {batch} ({el:.1f} s)",
-    }
+    return x.shape[0] * calls / el, calls, el
+
+
+def cpu_arms(n: int, steps: int, warmup: int, budget_s: float | None, one_thread_s: float = 3.0, sample=None):
+    """The reference's own CPU path (the installed package's adrt, all host
+    threads, then one thread) and the oracle port beside it, on the same
+    bounded sample.  Returns the cpu_baseline record."""
+    from oracle import oracle, ref
+
+    x = cpu_sample(n) if sample is None else sample
+    sample = f"{x.shape[0]} images of {n}x{n} float32 per call ({x.shape[0] // 2} uniform [0,1), {x.shape[0] // 2} ellipse phantoms)"
+    rec = {"unit": UNIT, "cpu_model": cpu_model(), "host_cpus": os.cpu_count(), "sample": sample}
+    port_v, _, _ = time_cpu(oracle.adrt, x, steps, 1, budget_s)
+    rec["port_value"] = port_v
+    rec["port_cores"] = oracle.threads()
+    try:
+        A = ref.load()
+    except Exception as e:  # a reference that fails to import is reported, not hidden
+        A, rec["reference_error"] = None, repr(e)[:200]
+    if A is None:
+        rec.update({"kind": "port", "value": port_v, "cores": oracle.threads(),
+                    "reference": "not installed on this host (make -C oracle install-ref)"})
+        return rec
+    omp = _OpenMP()
+    cores = omp.max_threads()
+    v, calls, el = time_cpu(A.adrt, x, steps, warmup, budget_s)
+    omp.set_threads(1)
+    try:
+        v1, calls1, el1 = time_cpu(A.adrt, x, 1, 1, one_thread_s)
+    finally:
+        omp.set_threads(cores)
+    rec.update({"kind": "reference", "value": v, "cores": cores, "calls": calls, "seconds": el,
+                "value_1thread": v1, "seconds_1thread": el1,
+                "implementation": "reference package adrt.adrt (installed from its sources, -O3 -fopenmp)"})
+    return rec
 
 
 def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1e-4, epochs=60, pc_h=5,
-             pc_tilt=-0.25, pc_samples=32):
+             pc_tilt=-0.25, pc_samples=32, repeats=3, check_every=2):
     """Batched CG on the normal equations of noisy 256 x 256 ellipse phantoms
-    (data b = adrt(x) + N(0, (1e-3 max|b|)^2)): plain CG against the learned
-    arms, all with the same stopping rule.
+    (data b = adrt(x) + N(0, (1e-3 max|b|)^2)): plain CG against three other
+    arms, all with the same stopping rule and the same convergence-check
+    interval (`check_every` iterations):
 
-    * conv_pcg: preconditioned CG with the learned convolution
-      preconditioner (a (2h+1)^2 kernel fit as a least-squares inverse of
-      A^T A on noise images with spectrum |w|^-0.25, untimed);
     * unet_start: plain CG from the encoder-decoder network's starting image
-      (network trained here first on pairs the method generates: phantom ->
-      adrt -> noise -> plain CG to 1e-5, untimed);
+      (the learned component: the network is trained here first, untimed, on
+      pairs the method generates: phantom -> adrt -> noise -> plain CG to
+      1e-5); the network's forward pass is inside the timed region;
+    * conv_pcg: preconditioned CG with a convolution preconditioner whose
+      (2h+1)^2 kernel is fitted by least squares as an inverse of A^T A on
+      noise images (untimed) -- a fitted filter, reported as its own arm;
     * unet_start_conv_pcg: both.
 
     Solves/s = test images / wall time to ||A^T(Ax-b)|| / ||A^T b|| <= tol
-    for every image by CG's residual recurrence (the network's forward pass
-    is inside the timed region); a solve counts only when the residual
-    recomputed from scratch afterwards (untimed) meets the tolerance.  Each
-    arm runs eagerly (a captured graph saved nothing at ~4 ms per iteration)
-    and checks convergence every `check_every` iterations: 4 for plain CG,
-    2 for the preconditioned arms, whose ~10 iterations make a coarse check
-    cost whole iterations.  learned_over_plain is the best learned arm's
+    for every image by CG's residual recurrence; a solve counts only when the
+    residual recomputed from scratch afterwards (untimed) meets the
+    tolerance.  Every arm is timed `repeats` times; the line gives the mean
+    and the range.  learned_over_plain is the encoder-decoder arm's mean
     solves/s over plain CG's."""
-    import adrt_gb300 as adrt
     from adrt_gb300 import cg as cgmod
     from adrt_gb300 import learned, precond
 
@@ -220,15 +340,12 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
         # The timed solve stops on CG's own residual recurrence; the reported
         # residuals are recomputed from scratch afterwards (untimed).
         return cgmod.cg(b_te, x0=x0, tol=tol, max_iters=500, graph=False, precond=M, residuals=False,
-                        check_every=4 if M is None else 2)
+                        check_every=check_every)
 
     def finish(res):
         res.normal_residual, res.data_residual = cgmod.residuals_of(b_te, res.x)
         return res
 
-    cgmod.cg(b_te[:16], tol=tol, max_iters=200, graph=True)  # warm
-    plain, t_plain = timed(solve)
-    plain = finish(plain)
     ref = cgmod.cg(b_te[:oracle_batch].double(), tol=1e-9, max_iters=3000)
 
     def err(x):
@@ -240,18 +357,21 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
         # (1 % slack for the float32 recomputation).
         return int((r.normal_residual <= 1.01 * tol).sum())
 
-    out = {
-        "workload": f"{n_test} noisy {n}x{n} ellipse phantoms, tol {tol:g} on the normal equations",
-        "plain_solves_s": solved(plain) / t_plain,
-        "plain_solved": solved(plain),
-        "plain_iters_mean": float(plain.iterations.float().mean()),
-        "plain_normal_residual_max": float(plain.normal_residual.max()),
-        "plain_data_residual_mean": float(plain.data_residual.mean()),
-        "plain_err_vs_float64_cg": err(plain.x),
-    }
-    def arm(name, res, t):
+    out = {"workload": f"{n_test} noisy {n}x{n} ellipse phantoms, tol {tol:g} on the normal equations",
+           "check_every": check_every, "repeats": repeats}
+    rates = {}
+
+    def arm(name, fn):
+        fn()  # warm (allocations, first launches)
+        runs = []
+        for _ in range(repeats):
+            res, t = timed(fn)
+            res = finish(res)
+            runs.append(solved(res) / t)
+        rates[name] = runs
         out.update({
-            f"{name}_solves_s": solved(res) / t,
+            f"{name}_solves_s": statistics.mean(runs),
+            f"{name}_solves_s_range": [min(runs), max(runs)],
             f"{name}_solved": solved(res),
             f"{name}_iters_mean": float(res.iterations.float().mean()),
             f"{name}_normal_residual_max": float(res.normal_residual.max()),
@@ -259,13 +379,12 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
             f"{name}_err_vs_float64_cg": err(res.x),
         })
 
+    arm("plain", solve)
     t0 = time.perf_counter()
     M = precond.fit(n, h=pc_h, samples=pc_samples, seed=0, device=dev, tilt=pc_tilt)
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
-    cgmod.cg(b_te[:16], tol=tol, max_iters=200, graph=True, precond=M)  # warm
-    pcg, t_pcg = timed(lambda: solve(M=M))
-    arm("conv_pcg", finish(pcg), t_pcg)
+    arm("conv_pcg", lambda: solve(M=M))
     lo, hi = M.symbol_range()
     out["conv_preconditioner"] = {"kernel": f"{2 * pc_h + 1}x{2 * pc_h + 1}", "fit_samples": pc_samples,
                                   "fit_noise_spectrum": f"|w|^{pc_tilt}",
@@ -278,17 +397,25 @@ def cg_bench(torch, dev, n=256, n_train=4096, n_test=512, oracle_batch=64, tol=1
     net = learned.PreconditionerNet(dev, seed=0)
     log = learned.train(net, b_tr, x_tr, epochs=epochs, batch=16, lr=3e-4)
     del b_tr, x_tr
-    learned.learned_cg(net, b_te[:16], tol=tol, max_iters=200)  # warm
-    lrn, t_lrn = timed(lambda: solve(x0=net.predict(b_te)))
-    arm("unet_start", finish(lrn), t_lrn)
-    learned.learned_cg(net, b_te[:16], tol=tol, max_iters=200, precond=M)  # warm
-    both, t_both = timed(lambda: solve(x0=net.predict(b_te), M=M))
-    arm("unet_start_conv_pcg", finish(both), t_both)
-    arms = {k: out[f"{k}_solves_s"] for k in ("conv_pcg", "unet_start", "unet_start_conv_pcg")}
-    best = max(arms, key=arms.get)
+    arm("unet_start", lambda: solve(x0=net.predict(b_te)))
+    arm("unet_start_conv_pcg", lambda: solve(x0=net.predict(b_te), M=M))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        net.predict(b_te)
+    torch.cuda.synchronize()
+    out["unet_forward_ms"] = 1e3 * (time.perf_counter() - t0) / repeats
+
+    def ratio(name):
+        a, p = rates[name], rates["plain"]
+        return {"mean": statistics.mean(a) / statistics.mean(p), "range": [min(a) / max(p), max(a) / min(p)]}
+
     out.update({
-        "learned_best": best,
-        "learned_over_plain": arms[best] / out["plain_solves_s"],
+        "learned_arm": "unet_start (encoder-decoder starting image, plain CG)",
+        "learned_over_plain": ratio("unet_start")["mean"],
+        "learned_over_plain_range": ratio("unet_start")["range"],
+        "conv_pcg_over_plain": ratio("conv_pcg"),
+        "unet_start_conv_pcg_over_plain": ratio("unet_start_conv_pcg"),
         "training": {"pairs": n_train, "pair_seconds": t_pairs, "epochs": epochs, "steps": log.steps,
                      "seconds": log.seconds, "loss_first": log.losses[0], "loss_last": log.losses[-1]},
     })
@@ -345,7 +472,7 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
         e = [rel(fmg[k], imgs[i]) for k, i in enumerate(sub) if imgs[i].shape[-1] == n]
         if e:
             err_fmg[str(n)] = float(np.median(e))
-    return {
+    rec = {
         "workload": f"{count} float32 ellipse phantoms, n from {{32..1024}} weights .3/.25/.2/.15/.07/.03",
         "counts": {str(n): sum(1 for m in imgs if m.shape[-1] == n) for n in sizes},
         "adrt_img_s": count / t_fwd,
@@ -356,6 +483,49 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
         "iadrt_rel_err_vs_input_median": err_inv,
         "iadrt_fmg_rel_err_vs_input_median": err_fmg,
     }
+    # One image of every size, with this library's results, for the comparison
+    # with the reference's own inverses in the CPU-baseline leg.
+    first = {}
+    for i, m in enumerate(imgs):
+        first.setdefault(int(m.shape[-1]), i)
+    fmg_of = {i: k for k, i in enumerate(sub)}
+    check = [(n, ys[i].cpu().numpy(), inv[i].cpu().numpy(), fmg[fmg_of[i]].cpu().numpy() if i in fmg_of else None)
+             for n, i in sorted(first.items())]
+    return rec, check
+
+
+def reference_inverse_checks(check):
+    """Relative errors of this library's ragged inverses against the
+    reference's own (its adrt.iadrt and adrt.iadrt_fmg on the host), one
+    image per size.  Part of the CPU-baseline leg: the reference is the
+    checker here."""
+    import numpy as np
+
+    from oracle import ref
+
+    A = ref.load()
+    if A is None:
+        return {"reference": "not installed on this host"}
+
+    def rel(a, b):
+        b = b.astype(np.float64)
+        d = np.linalg.norm(a.astype(np.float64) - b)
+        nb = np.linalg.norm(b)
+        return float(d / nb) if nb > 0 else float(d)
+
+    out = {}
+    for n, y, inv, fmg in check:
+        t0 = time.perf_counter()
+        r_inv = A.iadrt(y)
+        e = {"iadrt_rel_err_vs_reference": rel(inv, r_inv),
+             "iadrt_bit_exact": bool(np.array_equal(inv.view(np.uint32), r_inv.view(np.uint32)))}
+        if fmg is not None:
+            r_fmg = A.iadrt_fmg(y)
+            e["iadrt_fmg_rel_err_vs_reference"] = rel(fmg, r_fmg)
+            e["iadrt_fmg_max_abs_diff"] = float(np.max(np.abs(fmg.astype(np.float64) - r_fmg)))
+        e["seconds"] = time.perf_counter() - t0
+        out[str(n)] = e
+    return out
 
 
 def autograd_bench(torch, dev, batch=64, n=512, steps=5):
@@ -394,43 +564,29 @@ def autograd_bench(torch, dev, batch=64, n=512, steps=5):
 
 
 def run_reference(args):
+    """The reference arm: the reference package's own adrt.adrt on the host
+    cores (all threads), on a bounded sample of this benchmark's workload,
+    `--steps` timed calls after `--warmup` untimed ones.  Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import numpy as np
-
-    from oracle import oracle
-
-    kind = "port"
-    fn = oracle.adrt
-    try:
-        from oracle import ref
-
-        A = ref.load()
-        if A is not None:
-            fn, kind = A.adrt, "reference"
-    except Exception:
-        pass
-    sample = 8
-    x = np.random.default_rng(0).random((sample, args.n, args.n), dtype=np.float32)
-    for _ in range(args.warmup):
-        fn(x)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        fn(x)
-    el = time.perf_counter() - t0
-    value = sample * args.steps / el
+    cb = cpu_arms(args.n, args.steps, args.warmup, None)
+    value = cb["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1000 * cpu_sample_size() / value, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_images_per_step": sample, "n": args.n},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.threads(), "kind": kind,
-                         "sample": f"{sample} images of {args.n}x{args.n} float32 per step"},
+        "config": {"workload": WORKLOAD, "n": args.n, "sample_images_per_step": cpu_sample_size(),
+                   "inputs": "half uniform [0,1), half random-ellipse phantoms"},
+        "cpu_baseline": cb,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_sample_size() -> int:
+    return 8
 
 
 def main():
@@ -523,6 +679,11 @@ def main():
     clocks = sampler.stop() if sampler else None
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1000.0)
     value = world * B * args.steps / t_dev
+    # Four images of each half of the batch and their timed results (copied
+    # out after the timed region) for the CPU-baseline leg.
+    pick = [0, 1, 2, 3, B // 2, B // 2 + 1, B // 2 + 2, B // 2 + 3] if B >= 8 else list(range(B))
+    parity_x = x[pick].cpu().numpy()
+    parity_y = y[pick].cpu().numpy()
     del y
 
     # ---- end to end through host buffers ----------------------------------
@@ -569,40 +730,62 @@ def main():
         }
         del yh
 
+    peak, peak_src = load_peaks()
     extras = {}
     if not args.no_extras:
-        yd = adrt.adrt(x)
-        for _ in range(3):
-            z = adrt.bdrt(yd)
-        torch.cuda.synchronize()
-        e0.record(stream)
+        def dev_time(fn, reps):
+            for _ in range(3):
+                r = fn()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                r = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return r, e0.elapsed_time(e1) / 1000.0 / reps
+
+        def roof(img_s, bpi):
+            a = img_s * bpi / 1e9
+            return {"bound": "hbm", "achieved": a, "peak": peak, "unit": "GB/s", "frac": a / peak,
+                    "bytes_per_image": bpi, "peak_source": peak_src}
+
         ks = max(3, args.steps // 3)
-        for _ in range(ks):
-            z = adrt.bdrt(yd)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        extras["bdrt_img_s"] = B * ks / (e0.elapsed_time(e1) / 1000.0)
-        del z, yd
+        yd = adrt.adrt(x)
+        z, t = dev_time(lambda: adrt.bdrt(yd), ks)
+        extras["bdrt_img_s"] = B / t
+        extras["bdrt"] = {"workload": f"bdrt of the {B} x (4, {2 * n - 1}, {n}) float32 forward outputs",
+                          "img_s": B / t, "roofline": roof(B / t, 2 * bytes_per_image_bdrt(n, 4))}
+        del z
+        yi = yd[:64].contiguous()
+        del yd
+        inv, t = dev_time(lambda: adrt.iadrt(yi), ks)
+        extras["iadrt"] = {"workload": f"iadrt of 64 x (4, {2 * n - 1}, {n}) float32", "img_s": 64 / t,
+                           "roofline": roof(64 / t, 2 * bytes_per_image_bdrt(n, 4)),
+                           "bound_note": "serial chains of 2n-1 dependent adds per stage (latency)"}
+        del inv, yi
         x64 = x[:64].double()
-        for _ in range(3):
-            y64 = adrt.adrt(x64)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(ks):
-            y64 = adrt.adrt(x64)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        t64 = e0.elapsed_time(e1) / 1000.0
-        extras["adrt_f64_img_s"] = 64 * ks / t64
-        extras["adrt_f64_gbs"] = 64 * ks * bytes_per_image(n, 8) / t64 / 1e9
+        y64, t64 = dev_time(lambda: adrt.adrt(x64), ks)
+        extras["adrt_f64_img_s"] = 64 / t64
+        extras["adrt_f64_gbs"] = 64 * bytes_per_image(n, 8) / t64 / 1e9
+        rate = dadd_rate(torch, dev, _lib)
+        adds = min_adds_per_image(n)
+        extras["adrt_f64"] = {
+            "workload": f"adrt of 64 x {n}x{n} float64", "img_s": 64 / t64,
+            "roofline_hbm": roof(64 / t64, bytes_per_image(n, 8)),
+            "roofline_fp64": {"bound": "fp64 add pipe", "achieved": 64 / t64 * adds / 1e12,
+                              "peak": rate / 1e12, "unit": "Tadd/s", "frac": 64 / t64 * adds / rate,
+                              "adds_per_image": adds, "img_s_roof": rate / adds,
+                              "peak_how": "adrt_gb300_probe_dadd: 152x8 CTAs x 256 threads, 8 independent "
+                                          "round-to-nearest add chains each, CUDA events"},
+        }
         del y64, x64
 
+    ragged_check = None
     if not args.no_extras and rank == 0:
         extras["autograd"] = autograd_bench(torch, dev)
-        extras["ragged"] = ragged_bench(torch, dev)
+        extras["ragged"], ragged_check = ragged_bench(torch, dev)
         extras["cg"] = cg_bench(torch, dev)
 
-    peak, peak_src = load_peaks()
     bpi = bytes_per_image(n, 4)
     achieved = value / world * bpi / 1e9
     traffic = load_traffic(WORKLOAD)
@@ -645,7 +828,13 @@ def main():
     }
     line.update(extras)
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
-        line["cpu_baseline"] = cpu_baseline_run(n, "float32", args.cpu_seconds)
+        # CPU-baseline leg: the reference timed on a sample of this very batch,
+        # and used as the checker of the GPU results for those images.
+        cb = cpu_arms(n, 0, 1, args.cpu_seconds, sample=parity_x)
+        cb["parity_vs_reference"] = sample_parity(parity_x, parity_y)
+        if ragged_check is not None:
+            cb["ragged_inverses_vs_reference"] = reference_inverse_checks(ragged_check)
+        line["cpu_baseline"] = cb
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -86,6 +86,13 @@ void adrt_gb300_tune_reset(void);
  * otherwise.  No reference counterpart. */
 int adrt_gb300_device_status(void *stream);
 
+/* Measurement kernel (no reference counterpart): `blocks` x `threads`
+ * threads each perform 8 x `iters` float64 adds (8 independent chains of
+ * round-to-nearest adds) and write one double each to out (blocks x threads
+ * doubles).  Timed by the caller, it gives the GPU's float64 add rate, the
+ * roof of the float64 transforms. */
+int adrt_gb300_probe_dadd(double *out, int blocks, int threads, int iters, void *stream);
+
 /* Bytes of workspace that `op` needs for `batch` arrays of side n.  May be 0.
  * The reference allocates this temporary itself with PyMem_Malloc
  * (src/adrt/adrt_cdefs_py.cpp:301-307). */

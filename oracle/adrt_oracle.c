@@ -7,10 +7,10 @@
  * into it (the Python package raises when its CUDA library is missing).
  *
  * Parity of this restatement is pinned two ways:
- *   - bit-for-bit against the reference's own compiled extension (built from
- *     its sources by oracle/Makefile into oracle/_ref/, see
- *     tests/test_oracle_vs_reference.py) on random inputs, signed zeros and
- *     edge sizes;
+ *   - bit-for-bit against the reference package itself (installed into
+ *     baseline/_ref and its extension compiled from its own sources by
+ *     oracle/Makefile, see tests/test_oracle_reference.py) on random inputs,
+ *     signed zeros and edge sizes;
  *   - against the golden fixtures under tests/golden/, which were generated
  *     by that same compiled reference (tests/golden/make_golden.py).
  *

@@ -1,28 +1,30 @@
-"""Loader for the reference adrt package, compiled from its own sources.
+"""Loader for the reference adrt package installed in baseline/_ref.
 
-TEST INFRASTRUCTURE ONLY.  ``make -C oracle ref`` compiles the reference's
-CPython extension from the reference checkout into ``oracle/_ref/``; this
-module imports the reference's Python package from that checkout with the
-compiled extension attached.  It is available only on a machine that has the
-reference checkout (not on the GPU host); callers must handle ``None``.
+TEST AND BASELINE INFRASTRUCTURE ONLY.  ``make -C oracle install-ref
+REF_SRC=<adrt checkout>`` installs the reference package (its Python modules
+and C++ sources) into the git-ignored ``baseline/_ref/adrt`` and compiles its
+CPython extension there; ``make -C oracle ref`` recompiles the extension on a
+host of another architecture.  This module imports that package unmodified,
+so callers use the reference's own public API (``adrt.adrt`` and so on).
+``ADRT_REFERENCE_INSTALL`` overrides the install directory.  Returns None
+where the package or its compiled extension is absent; callers handle that.
 """
 
 from __future__ import annotations
 
 import glob
-import importlib.machinery
 import importlib.util
 import os
 import sys
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("ADRT_REFERENCE_ROOT", "/root/reference")
+REF_DIR = os.environ.get("ADRT_REFERENCE_INSTALL", os.path.join(os.path.dirname(_HERE), "baseline", "_ref"))
 _cached = None
 
 
-def _ext_path():
-    hits = glob.glob(os.path.join(_HERE, "_ref", "_adrt_cdefs*.so"))
-    return hits[0] if hits else None
+def available() -> bool:
+    pkg = os.path.join(REF_DIR, "adrt")
+    return os.path.isfile(os.path.join(pkg, "__init__.py")) and bool(glob.glob(os.path.join(pkg, "_adrt_cdefs*.so")))
 
 
 def load():
@@ -30,28 +32,21 @@ def load():
     global _cached
     if _cached is not None:
         return _cached
-    src = os.path.join(REF_ROOT, "src", "adrt")
-    ext = _ext_path()
-    if not os.path.isdir(src) or ext is None:
+    if not available():
         return None
-    # Load the compiled extension under the name the package expects, then the
-    # package itself from the (read-only) checkout.
-    loader = importlib.machinery.ExtensionFileLoader("adrt._adrt_cdefs", ext)
-    spec = importlib.util.spec_from_file_location("adrt._adrt_cdefs", ext, loader=loader)
-    cdefs = importlib.util.module_from_spec(spec)
-    loader.exec_module(cdefs)
-    saved = sys.modules.get("adrt")
-    pkg_spec = importlib.util.spec_from_file_location(
-        "adrt", os.path.join(src, "__init__.py"), submodule_search_locations=[src]
+    pkg_dir = os.path.join(REF_DIR, "adrt")
+    saved = {k: sys.modules[k] for k in list(sys.modules) if k == "adrt" or k.startswith("adrt.")}
+    spec = importlib.util.spec_from_file_location(
+        "adrt", os.path.join(pkg_dir, "__init__.py"), submodule_search_locations=[pkg_dir]
     )
-    pkg = importlib.util.module_from_spec(pkg_spec)
+    pkg = importlib.util.module_from_spec(spec)
     sys.modules["adrt"] = pkg
-    sys.modules["adrt._adrt_cdefs"] = cdefs
     try:
-        pkg_spec.loader.exec_module(pkg)
+        spec.loader.exec_module(pkg)
     except Exception:
-        if saved is not None:
-            sys.modules["adrt"] = saved
+        for k in [k for k in sys.modules if k == "adrt" or k.startswith("adrt.")]:
+            del sys.modules[k]
+        sys.modules.update(saved)
         raise
     _cached = pkg
     return pkg

@@ -32,7 +32,7 @@ def signed_zero_image(rng, n, dtype):
 def main() -> None:
     A = ref.load()
     if A is None:
-        raise SystemExit("reference not available: run `make -C oracle ref` with the checkout present")
+        raise SystemExit("reference not available: run `make -C oracle install-ref REF_SRC=<adrt checkout>`")
     out = {}
     # Small uniform [0,1) image: 64 x 64 float32, seed 0; adrt and bdrt of it.
     x = np.random.default_rng(0).random((64, 64), dtype=np.float32)

@@ -26,7 +26,7 @@ from oracle import ref  # noqa: E402
 def main() -> None:
     A = ref.load()
     if A is None:
-        raise SystemExit("reference not available: run `make -C oracle ref` with the checkout present")
+        raise SystemExit("reference not available: run `make -C oracle install-ref REF_SRC=<adrt checkout>`")
     out = {}
     rng = np.random.default_rng(4321)
     for dt in ("float32", "float64"):

@@ -1,6 +1,7 @@
-"""Cross-checks the CPU oracle against the reference package compiled from its
-own sources (oracle/_ref, built by ``make -C oracle ref``).  Skipped where the
-reference checkout is not present (e.g. on the GPU host)."""
+"""Cross-checks the CPU oracle against the reference package itself (installed
+into baseline/_ref by ``make -C oracle install-ref``, its extension compiled
+from its own sources by ``make -C oracle ref``).  Skipped where that install
+is absent."""
 
 import numpy as np
 import pytest
@@ -14,7 +15,7 @@ def ref():
 
     A = refmod.load()
     if A is None:
-        pytest.skip("reference package not built here (make -C oracle ref)")
+        pytest.skip("reference package not installed here (make -C oracle install-ref)")
     return A
 
 
