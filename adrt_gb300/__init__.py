@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import collections.abc
 import math
+import operator
+import sys
 import typing
 
 import torch
@@ -43,6 +45,24 @@ def _residual_norm(x: torch.Tensor, a: torch.Tensor, ws: torch.Tensor, acc: torc
     return math.sqrt(float(acc.item()))
 
 
+def _iteration_limit(max_iters):
+    """max_iters as an int (None: unbounded).  The reference checks `< 1`
+    first, then hands the value to itertools.islice, which takes only None or
+    an index in [0, sys.maxsize] and raises ValueError otherwise; the same
+    values are accepted and rejected here."""
+    if max_iters is not None and max_iters < 1:
+        raise ValueError(f"must allow at least one iteration, but specified {max_iters}")
+    if max_iters is None:
+        return None
+    try:
+        limit = operator.index(max_iters)
+    except TypeError:
+        limit = -1
+    if not 0 <= limit <= sys.maxsize:
+        raise ValueError(f"max_iters must be None or an integer in [0, {sys.maxsize}], got {max_iters!r}")
+    return limit
+
+
 def iadrt_fmg_batched(a, /, *, max_iters: int | None = None):
     """iadrt_fmg for every (4, 2n-1, n) array of a batch (B, 4, 2n-1, n) at
     once (not in the reference, whose iadrt_fmg takes one array): the images
@@ -50,8 +70,7 @@ def iadrt_fmg_batched(a, /, *, max_iters: int | None = None):
     is bit-identical to iadrt_fmg of that image alone (the same kernels, and
     per-image residual norms summed with the single-array partition).
     Returns (B, n, n)."""
-    if max_iters is not None and max_iters < 1:
-        raise ValueError(f"must allow at least one iteration, but specified {max_iters}")
+    max_iters = _iteration_limit(max_iters)
     if a.ndim != 4:
         raise ValueError(f"iadrt_fmg_batched expects a batch (B, 4, 2n-1, n), got {a.ndim} dimensions")
     st = Staged(a)
@@ -94,8 +113,7 @@ def iadrt_fmg(a, /, *, max_iters: int | None = None):
     strictly smaller residual norm; the norm is accumulated in float64)."""
     if a.ndim > 3:
         raise ValueError(f"batch dimension not supported for iadrt_fmg, got {a.ndim} dimensions")
-    if max_iters is not None and max_iters < 1:
-        raise ValueError(f"must allow at least one iteration, but specified {max_iters}")
+    max_iters = _iteration_limit(max_iters)
     st = Staged(a)
     t = st.t
     ws = torch.empty(_lib.load().adrt_gb300_sumsq_workspace_size(), dtype=torch.uint8, device=st.device)

@@ -447,10 +447,10 @@ __device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, i
 // bank groups when writing, and a row's eight chunks are distinct when read.
 
 template <int L1>
-__device__ __forceinline__ void group2_passB(const float *xs, float *ost, int c0, int n) {
-  // A half whose first stored offset is past the end stores nothing: the
-  // staged rows the store loop reads all come from the other half.
-  const bool idle = c0 + 8 * first_stored_block() >= 2 * n - 1;
+__device__ __forceinline__ void group2_passB(const float *xs, float *ost, int live) {
+  // A half whose first stored offset is at or past `live` stages nothing: the
+  // store loop writes +0 for those rows.
+  const bool idle = 8 * first_stored_block() >= live;
   int b;
   bool active, store;
   group2_lane(b, active, store);
@@ -467,15 +467,14 @@ __device__ __forceinline__ void group2_passB(const float *xs, float *ost, int c0
     *reinterpret_cast<float4 *>(p0 + 32 * k) = make_float4(out[0][k], out[1][k], out[2][k], out[3][k]);
     *reinterpret_cast<float4 *>(p1 + 32 * k) = make_float4(out[4][k], out[5][k], out[6][k], out[7][k]);
   }
-  (void)c0;
-  (void)n;
 }
 
 // Writes the staged tile: quarter-warps store one 128-byte row each.  Thread
 // t handles chunk t & 7 of rows (t >> 3) + 32 i, i < W / 32; the row's swizzle
 // term ((row >> 3) & 7) then only alternates between two values.  All shared
-// loads are issued before the global stores.
-__device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q, int ap, int c0, int n) {
+// loads are issued before the global stores.  Rows at or past `live` are +0
+// (offsets beyond every angle's support) and are not read from the staging.
+__device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q, int ap, int c0, int n, int live) {
   constexpr int IT = W / 32;  // 15
   static_assert(W % 32 == 0, "tile rows must split into 32-row steps");
   const int r0 = threadIdx.x >> 3, c = threadIdx.x & 7;
@@ -485,7 +484,8 @@ __device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q,
   float4 v[IT];
 #pragma unroll
   for (int i = 0; i < IT; ++i)
-    v[i] = *reinterpret_cast<const float4 *>((i & 1 ? s1 : s0) + (i >> 1) * 64 * 32);
+    v[i] = r0 + 32 * i < live ? *reinterpret_cast<const float4 *>((i & 1 ? s1 : s0) + (i >> 1) * 64 * 32)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
   const int rows = min(W, 2 * n - 1 - c0);
   float *d = dst_q + (size_t)(c0 + r0) * n + ap * 32 + 4 * c;
   const size_t step = (size_t)32 * n;
@@ -539,10 +539,21 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
   const int bimg = t % nimg;
   const int ap = t / nimg;
   const int c0 = ct * W, tbase = c0 - HALO;
+  float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
+  // Every final angle of this CTA is below 32 a' + 32, and at angle a the
+  // output is +0 at offsets >= n + a (beyond the support of every digital
+  // line); offsets from `lim` on are +0 at all 32 angles.  Tiles past it only
+  // store zeros; a tile that reaches it computes only the live rows.
+  const int lim = min(2 * n - 1, n + 32 * ap + 31);
+  const int live = min(W, lim - c0);
+  if (live <= 0) {
+    passB_store_tile(xs, dst_q, ap, c0, n, 0);
+    return;
+  }
   // member j row: inter[bimg][q][j][ap][*]
   const size_t mstride = (size_t)a_in * cs;
   const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * a_in + ap) * cs;
-  const int pos = needed_positions(min(W, 2 * n - 1 - c0));
+  const int pos = needed_positions(live);
   (void)err;
   switch (ap & 3) {
     case 0: group1_passB<0>(src, ap, tbase, pos, xs, mstride, cs); break;
@@ -551,17 +562,16 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
     default: group1_passB<3>(src, ap, tbase, pos, xs, mstride, cs); break;
   }
   __syncthreads();
-  float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
   // The output tile is staged over the exchange rows once all warps have
   // read them (barrier inside group2_passB).
   switch ((threadIdx.x >> 5) & 3) {
-    case 0: group2_passB<0>(xs, xs, c0, n); break;
-    case 1: group2_passB<1>(xs, xs, c0, n); break;
-    case 2: group2_passB<2>(xs, xs, c0, n); break;
-    default: group2_passB<3>(xs, xs, c0, n); break;
+    case 0: group2_passB<0>(xs, xs, live); break;
+    case 1: group2_passB<1>(xs, xs, live); break;
+    case 2: group2_passB<2>(xs, xs, live); break;
+    default: group2_passB<3>(xs, xs, live); break;
   }
   __syncthreads();
-  passB_store_tile(xs, dst_q, ap, c0, n);
+  passB_store_tile(xs, dst_q, ap, c0, n, live);
 }
 
 }  // namespace fast
