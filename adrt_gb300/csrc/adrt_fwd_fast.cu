@@ -50,7 +50,6 @@ static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange
 
 __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
 
-__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ float4 ld4_stream(const float *p) {
   return __ldcs(reinterpret_cast<const float4 *>(p));
 }
@@ -168,17 +167,42 @@ __device__ __forceinline__ void put_exchange(float *xs, int mq, int ch, const fl
   }
 }
 
+// Chunk load with a fill value: a lane whose chunk lies outside [0, lim)
+// gets the fill (-0 before the start: absent operands; +0 past the end: the
+// zero padding and its sums) and issues no memory access.  Predicated in PTX
+// so that the three cases cost no divergent branches.  STREAM: evict-first
+// (data read once); otherwise default caching (the image, which all four
+// quadrants read).
+template <bool STREAM>
+__device__ __forceinline__ float4 ld4_fill(const float *p, int g0, int lim) {
+  float4 v;
+  const float fill = __int_as_float(g0 & (int)0x80000000);
+  const unsigned in = (unsigned)g0 < (unsigned)lim;
+  if (STREAM)
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\tmov.b32 %0, %6;\n\tmov.b32 %1, %6;\n\t"
+        "mov.b32 %2, %6;\n\tmov.b32 %3, %6;\n\t@q ld.global.cs.v4.f32 {%0, %1, %2, %3}, [%4];\n\t}"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p), "r"(in), "f"(fill));
+  else
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\tmov.b32 %0, %6;\n\tmov.b32 %1, %6;\n\t"
+        "mov.b32 %2, %6;\n\tmov.b32 %3, %6;\n\t@q ld.global.v4.f32 {%0, %1, %2, %3}, [%4];\n\t}"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p), "r"(in), "f"(fill));
+  return v;
+}
+
 // Loads of group 1 are all issued before any of them is consumed: a warp
 // holds its whole sweep (4-5 chunks per member) in registers, so the load
 // latency is paid once per tile rather than once per iteration.
 
 // Pass A, quadrants 0 and 3: members are image rows, positions run along the
 // row from its right end (offset c <-> column n-1-c).  Warp = member quad.
+template <int NIT = 0>
 __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase, int pos,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
   constexpr int IT = NCH / 32;
-  const int nit = sweep_iters(pos);
+  const int nit = NIT ? NIT : sweep_iters(pos);
   float4 raw[IT][4];
 #pragma unroll
   for (int it = 0; it < IT; ++it) {
@@ -188,9 +212,7 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
     for (int jj = 0; jj < 4; ++jj) {
       const int R0 = 32 * r + 4 * mq + jj;
       const int irow = (q == 0) ? R0 : (N - 1 - R0);
-      if (ref0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
-      else if (ref0 >= N) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
-      else raw[it][jj] = ld4(img + (size_t)irow * N + (N - 4 - ref0));
+      raw[it][jj] = ld4_fill<false>(img + irow * N + (N - 4 - ref0), ref0, N);
     }
   }
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
@@ -231,9 +253,8 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
     for (int k = 0; k < 4; ++k) {
       const int ref = ref0 + k;
       const int irow = (q == 2) ? ref : (N - 1 - ref);
-      if (!live || ref < 0) raw[it][k] = make_float4(-0.f, -0.f, -0.f, -0.f);
-      else if (ref >= N) raw[it][k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      else raw[it][k] = ld4(img + (size_t)irow * N + 32 * r + 4 * mq);
+      // A chunk past this warp's range only seeds nothing: load it as absent.
+      raw[it][k] = ld4_fill<false>(img + irow * N + 32 * r + 4 * mq, live ? ref : -1, N);
     }
   }
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
@@ -258,12 +279,13 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
 // compile-time constant per A4 = a' mod 4, so the realignment is a fixed
 // selection of this lane's and the previous lane's 16-byte chunk.  Slot 0 of
 // `raw` holds the chunk that precedes the first one, seeding lane 0.
-template <int A4>
+// NIT: sweep iterations when known at compile time (full tiles), else 0.
+template <int A4, int NIT = 0>
 __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase, int pos, float *xs,
                                              size_t mstride, int cs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
   constexpr int IT = NCH / 32;
-  const int nit = sweep_iters(pos);
+  const int nit = NIT ? NIT : sweep_iters(pos);
   float4 raw[IT + 1][4];
 #pragma unroll
   for (int jj = 0; jj < 4; ++jj) {
@@ -284,9 +306,7 @@ __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase
         if (it > nit) break;
         // slot 0: the chunk before chunk 0 (only lane 31's copy is used)
         const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
-        if (g0 < 0) raw[it][jj] = make_float4(-0.f, -0.f, -0.f, -0.f);
-        else if (g0 >= cs) raw[it][jj] = make_float4(0.f, 0.f, 0.f, 0.f);
-        else raw[it][jj] = ld4_stream(row + g0);
+        raw[it][jj] = ld4_fill<true>(row + g0, g0, cs);
       }
     }
   }
@@ -506,8 +526,12 @@ __global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__
   const int c0 = ct * W, tbase = c0 - HALO;
   const int pos = needed_positions(min(W, CS - c0));
   const float *img = in + (size_t)bimg * N * N;
-  if (q == 0 || q == 3) group1_passA_rows(img, q, r, tbase, pos, xs);
-  else group1_passA_cols(img, q, r, tbase, pos, xs);
+  if (q == 0 || q == 3) {
+    if (pos == TW) group1_passA_rows<NCH / 32>(img, q, r, tbase, pos, xs);
+    else group1_passA_rows(img, q, r, tbase, pos, xs);
+  } else {
+    group1_passA_cols(img, q, r, tbase, pos, xs);
+  }
   __syncthreads();
   float *dst_rows = inter + ((size_t)(bimg * 4 + q) * 32 + r) * 32 * CS;
   switch ((threadIdx.x >> 5) & 3) {
@@ -528,16 +552,13 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
                                                        int col_tiles, unsigned *err) {
   extern __shared__ __align__(16) float xs[];
   const int a_in = n / 32;
-  // Block order: column tile fastest, then quadrant, image, and the input
-  // angle a' slowest, so the CTAs resident on an SM at a time mostly share
-  // a' mod 4 and run the same group-1 code (measured 4 % faster than a'
-  // second-fastest, through fewer instruction-cache misses).
-  int t = blockIdx.x;
-  const int nimg = (int)(gridDim.x / (unsigned)(4 * a_in * col_tiles));
-  const int ct = t % col_tiles; t /= col_tiles;
-  const int q = t % 4; t /= 4;
-  const int bimg = t % nimg;
-  const int ap = t / nimg;
+  // Grid (column tile + col_tiles * quadrant, image, input angle a'): the
+  // input angle is the slowest launch dimension, so the CTAs resident on an
+  // SM at a time mostly share a' mod 4 and run the same group-1 code
+  // (measured 4 % faster than a' second-fastest, through fewer
+  // instruction-cache misses).
+  const int ct = (int)(blockIdx.x % (unsigned)col_tiles), q = (int)(blockIdx.x / (unsigned)col_tiles);
+  const int bimg = (int)blockIdx.y, ap = (int)blockIdx.z;
   const int c0 = ct * W, tbase = c0 - HALO;
   float *dst_q = out + (size_t)(bimg * 4 + q) * (2 * n - 1) * n;
   // Every final angle of this CTA is below 32 a' + 32, and at angle a the
@@ -555,11 +576,20 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
   const float *src = inter + ((size_t)(bimg * 4 + q) * 32 * a_in + ap) * cs;
   const int pos = needed_positions(live);
   (void)err;
-  switch (ap & 3) {
-    case 0: group1_passB<0>(src, ap, tbase, pos, xs, mstride, cs); break;
-    case 1: group1_passB<1>(src, ap, tbase, pos, xs, mstride, cs); break;
-    case 2: group1_passB<2>(src, ap, tbase, pos, xs, mstride, cs); break;
-    default: group1_passB<3>(src, ap, tbase, pos, xs, mstride, cs); break;
+  if (pos == TW) {  // full tile: the sweep length is a compile-time constant
+    switch (ap & 3) {
+      case 0: group1_passB<0, NCH / 32>(src, ap, tbase, pos, xs, mstride, cs); break;
+      case 1: group1_passB<1, NCH / 32>(src, ap, tbase, pos, xs, mstride, cs); break;
+      case 2: group1_passB<2, NCH / 32>(src, ap, tbase, pos, xs, mstride, cs); break;
+      default: group1_passB<3, NCH / 32>(src, ap, tbase, pos, xs, mstride, cs); break;
+    }
+  } else {
+    switch (ap & 3) {
+      case 0: group1_passB<0>(src, ap, tbase, pos, xs, mstride, cs); break;
+      case 1: group1_passB<1>(src, ap, tbase, pos, xs, mstride, cs); break;
+      case 2: group1_passB<2>(src, ap, tbase, pos, xs, mstride, cs); break;
+      default: group1_passB<3>(src, ap, tbase, pos, xs, mstride, cs); break;
+    }
   }
   __syncthreads();
   // The output tile is staged over the exchange rows once all warps have
@@ -597,6 +627,7 @@ static i64 fast_chunk(i64 batch, i64 n) {
   const int mb = tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).chunk_mb;
   i64 k = (i64)(((size_t)(mb > 0 ? mb : 4096) << 20) / fast_inter_bytes(n));
   if (k < 1) k = 1;
+  if (k > 65535) k = 65535;  // images are pass B's grid y dimension
   if (batch <= k) return batch;
   const i64 nchunks = (batch + k - 1) / k;
   return (batch + nchunks - 1) / nchunks;
@@ -653,7 +684,7 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
       rc = fwd_first_pass_padded(in + b0 * n * n, inter, nb, n, L - 5, cs, st);
     }
     if (rc) return rc;
-    const unsigned gridb = (unsigned)(nb * 4 * (n / 32) * col_tiles);
+    const dim3 gridb((unsigned)(col_tiles * 4), (unsigned)nb, (unsigned)(n / 32));
     fast::pass_b_kernel<<<gridb, fast::NT, fast::SMEM, st>>>(inter, out + b0 * 4 * (2 * n - 1) * n, (int)n, cs,
                                                              col_tiles, err);
     rc = launch_status();
