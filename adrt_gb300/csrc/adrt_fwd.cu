@@ -111,6 +111,30 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
   const i64 c0 = (i64)ct * kFwdW;
   const i64 tbase = c0 - kFwdHalo;  // reference offset of tile position 0 (before pre-shift)
 
+  // Support: after k stages a row at angle a is +0 at offsets >= n + a (a
+  // digital line over the row group rises by at most a, and every term past
+  // the image is the +0 padding).  This pass's outputs have angles below
+  // (a'+1) 2^S, so from offset sup_out on the whole tile is +0: a last pass
+  // stores zeros there without computing, other passes skip the tile (the
+  // next pass bounds its loads by each input row's own support, n + a').  A
+  // padded fast-path intermediate (cs_out set) is read in whole 16-byte
+  // chunks up to its row length, so there every offset below cs_out is
+  // written.
+  const i64 sup_out = n + (ap + 1) * ROWS - 1;
+  const i64 skip_from = (!LAST && args.cs_out > sup_out) ? args.cs_out : sup_out;
+  if (c0 >= skip_from) {
+    if (LAST) {
+      T *dst = static_cast<T *>(args.out) + ((size_t)b * 4 + q) * (size_t)C * (unsigned)n + (unsigned)ap * ROWS;
+      for (int idx = threadIdx.x; idx < kFwdW * ROWS; idx += NT) {
+        const int l = idx % ROWS, w = idx / ROWS;
+        const int c = (int)c0 + w;
+        if (c < (int)C) st_stream(&dst[(unsigned)c * (unsigned)n + l], T(0));
+      }
+    }
+    return;
+  }
+  const int sup_in = (int)(FIRST ? n : (n + ap < C ? n + ap : C));
+
   // ---- load: member i, tile position u  <->  reference offset tbase + u - a'*i.
   // Offsets below 0 do not exist in the reference (it copies instead of adding
   // there); they are stored as -0.0, and e + (-0) == e for every e, so the
@@ -160,7 +184,7 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
       for (int u = lr; u < TWP; u += TL::TPR) {
         const int ref = rb + u;
         T v = ref < 0 ? T(-0.0) : T(0);
-        if (ref >= 0 && ref < (int)C) v = ld_l2(&rowp[ref]);
+        if (ref >= 0 && ref < sup_in) v = ld_l2(&rowp[ref]);
         buf0[i * RS + u] = v;
       }
     }
@@ -196,13 +220,15 @@ __device__ __forceinline__ void fwd_tile(const FwdPassArgs &args, i64 tile,
       if (c < (int)C) st_stream(&dst[(unsigned)c * un + l], cur[l * RS + kFwdHalo + w]);
     }
   } else {
+    // Rows of the buffer hold cs offsets (cs <= C: a padded fast-path
+    // intermediate keeps only its rows' supports).
     const unsigned cs = args.cs_out ? (unsigned)args.cs_out : (unsigned)C;
     T *dst = static_cast<T *>(args.out) + ((size_t)b * 4 + q) * un * (size_t)cs +
              ((size_t)r * A_out + (size_t)ap * ROWS) * cs + c0;
 #pragma unroll 4
     for (int idx = threadIdx.x; idx < ROWS * kFwdW; idx += NT) {
       const int l = idx / kFwdW, w = idx % kFwdW;
-      if ((int)c0 + w < (int)C) dst[(unsigned)l * cs + (unsigned)w] = cur[l * RS + kFwdHalo + w];
+      if ((unsigned)c0 + w < cs) dst[(unsigned)l * cs + (unsigned)w] = cur[l * RS + kFwdHalo + w];
     }
   }
 }

@@ -606,10 +606,13 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
 
 }  // namespace fast
 
-// Row stride of the fast path's intermediate: at n = 1024 the offsets pass A
-// writes (fast::CS); below, 2n-1 offsets rounded up to a multiple of 8 floats
-// (32 bytes) so every row start is 256-bit aligned.
-static int fast_cs(i64 n) { return n == fast::N ? fast::CS : (int)(((2 * n - 1) + 7) / 8 * 8); }
+// Row stride of the fast path's intermediate: the rows' support.  After the
+// first L-5 stages a row group's values are +0 at offsets >= n + n/32 - 1
+// (angles below n/32, each digital line rising by at most its angle), so the
+// rows end there, rounded up to 8 floats (32 bytes: every row start is 256-bit
+// aligned); pass B reads anything past the row end as +0.  n = 1024: 1056.
+static int fast_cs(i64 n) { return (int)((n + n / 32 - 1 + 7) / 8 * 8); }
+static_assert(fast::CS == (fast::N + fast::N / 32 - 1 + 7) / 8 * 8, "row stride at n = 1024");
 
 // Bytes of intermediate per image: [q][32][n/32][cs] float32.
 size_t fast_inter_bytes(i64 n) { return sizeof(float) * 4 * (size_t)n * fast_cs(n); }

@@ -98,6 +98,10 @@ def test_workspace_sizes(lib):
     per = 4 * 32 * 32 * 1056 * 4
     got = _lib.workspace_size(_lib.OP_ADRT, 256, 1024, _lib.F32)
     assert got > 0 and got % per == 0
+    # Below 1024 the first pass leaves L-5 stages done: rows end at n + n/32 - 1
+    # (rounded up to 8 floats): 528 at n = 512, 72 at n = 64.
+    for n, cs in ((512, 528), (256, 264), (128, 136), (64, 72)):
+        assert _lib.workspace_size(_lib.OP_ADRT, 3, n, _lib.F32) == 3 * 4 * n * cs * 4
     per64 = 4 * 512 * 1023 * 8
     got64 = _lib.workspace_size(_lib.OP_ADRT, 8, 512, _lib.F64)
     assert got64 > 0 and got64 % per64 == 0
