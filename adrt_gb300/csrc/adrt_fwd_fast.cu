@@ -60,16 +60,6 @@ __device__ __forceinline__ void st8(float *p, const float (&v)[8]) {
                : "memory");
 }
 
-// Two float32 adds in one packed instruction: d0 = a0 + b0, d1 = a1 + b1,
-// each rounded to nearest like add_rn (add.rn.f32x2 rounds per element).
-// Used where both operands of two neighbouring positions are adjacent
-// (butterfly shifts that are even).
-__device__ __forceinline__ void add_rn2(float a0, float a1, float b0, float b1, float &d0, float &d1) {
-  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d0), "=f"(d1)
-      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
-}
 
 // Value of `cur` held by the lane D below (the previous chunk).  Lanes whose
 // previous chunk was handled in the previous iteration (lane < D) receive the

@@ -39,6 +39,8 @@ struct BwdPassArgs {
   int k0;          // first forward stage covered by this pass
   i64 batch;
   i64 c_need;      // pass outputs are needed at reference offsets < c_need
+  i64 cs = 0;      // row stride of the bdrt buffers (0: 2n-1)
+  int c_begin = 0; // first tile position of this launch (tiles before it are done elsewhere)
 };
 
 // Buffer layout between passes, per (b, q): [angle s][section p][offset c],
@@ -64,10 +66,11 @@ struct BwdTile {
 
 // Column tiles of one pass: tile positions span [0, C + a'_max * (2^S - 1)) so
 // every member's pre-shifted window is covered.
-static __host__ __device__ inline int bwd_col_tiles(i64 n, int k0, int S, int W) {
+static __host__ __device__ inline int bwd_col_tiles(i64 n, int k0, int S, int W, int c_begin = 0) {
   const i64 C = 2 * n - 1;
   const i64 max_ext = ((i64(1) << k0) - 1) * ((1 << S) - 1);
-  return (int)((C + max_ext + W - 1) / W);
+  const i64 span = C + max_ext - c_begin;
+  return span > 0 ? (int)((span + W - 1) / W) : 0;
 }
 
 // Per-quadrant index arithmetic is 32-bit: a quadrant holds n (2n-1) < 2^32
@@ -88,7 +91,8 @@ bwd_pass_kernel(BwdPassArgs args) {
   const unsigned A_lo = 1u << k0;      // angles after this pass (pass output)
   const unsigned R_lo = n >> k0;       // sections after this pass
   const unsigned R_hi = R_lo >> S;     // sections at pass input
-  const int col_tiles = bwd_col_tiles(args.n, k0, S, W);
+  const int col_tiles = bwd_col_tiles(args.n, k0, S, W, args.c_begin);
+  const unsigned cs = args.cs ? (unsigned)args.cs : (unsigned)C;  // bdrt buffer row stride
 
   unsigned t = blockIdx.x;
   const int ct = (int)(t % (unsigned)col_tiles); t /= (unsigned)col_tiles;
@@ -96,11 +100,12 @@ bwd_pass_kernel(BwdPassArgs args) {
   const unsigned r = t % R_hi; t /= R_hi;
   const unsigned q = t & 3u; t >>= 2;
   const unsigned b = t;
-  const int c0 = ct * W;
+  const int c0 = args.c_begin + ct * W;
   // Skip tiles that hold no member's needed offsets (member i of this tile
   // stores reference offsets >= c0 - a'*i).
   if ((i64)c0 >= args.c_need + (i64)ap * (ROWS - 1)) return;
-  const size_t qoff = ((size_t)b * 4 + q) * (size_t)n * (size_t)C;  // quadrant base
+  const size_t qoff = ((size_t)b * 4 + q) * (size_t)n * (size_t)C;  // quadrant base, final layout
+  const size_t qbuf = ((size_t)b * 4 + q) * (size_t)n * (size_t)cs; // quadrant base, bdrt buffer
 
   // ---- load angle l = a'*2^S + l of section r, tile positions [c0, c0+TWP).
   if (FIRST) {
@@ -115,9 +120,9 @@ bwd_pass_kernel(BwdPassArgs args) {
       buf0[l * RS + u] = v;
     }
   } else {
-    const T *src = static_cast<const T *>(args.in) + qoff + ((size_t)ap * ROWS * R_hi + r) * C + c0;
+    const T *src = static_cast<const T *>(args.in) + qbuf + ((size_t)ap * ROWS * R_hi + r) * cs + c0;
     for (int l = threadIdx.x / TL::TPR; l < ROWS; l += TL::ROW_STEP) {
-      const T *rowp = src + (size_t)l * R_hi * (unsigned)C;
+      const T *rowp = src + (size_t)l * R_hi * cs;
 #pragma unroll 4
       for (int u = threadIdx.x % TL::TPR; u < TWP; u += TL::TPR) {
         T v = T(0);
@@ -181,9 +186,9 @@ bwd_pass_kernel(BwdPassArgs args) {
       if (c < C) st_stream(&dst[(unsigned)c * n + i], cur[i * RS + w]);
     }
   } else {
-    T *dst = static_cast<T *>(args.out) + qoff + ((size_t)ap * R_lo + r * ROWS) * C;
+    T *dst = static_cast<T *>(args.out) + qbuf + ((size_t)ap * R_lo + r * ROWS) * cs;
     for (int i = threadIdx.x / TL::TPR; i < ROWS; i += TL::ROW_STEP) {
-      T *rowp = dst + (size_t)i * (unsigned)C;
+      T *rowp = dst + (size_t)i * cs;
       const int cb = c0 - (int)ap * i;
 #pragma unroll 4
       for (int w = threadIdx.x % TL::TPR; w < W; w += TL::TPR) {
@@ -208,8 +213,9 @@ static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
   const i64 A_lo = i64(1) << a.k0;
-  const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W);
+  const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W, a.c_begin);
   const i64 tiles = a.batch * 4 * ((a.n >> a.k0) >> S) * A_lo * col_tiles;
+  if (tiles == 0) return ADRT_GB300_OK;
   kern<<<(unsigned)tiles, NT, smem, st>>>(a);
   return launch_status();
 }
@@ -235,12 +241,45 @@ static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cuda
   return bwd_dispatch_S<T, false, false>(S, a, st);
 }
 
+// Register-level passes (bdrt_fast.cu), float32, 256 <= n <= 1024: the last
+// bdrt pass (forward stages 0..4) for every such n, the first one (stages
+// 5..9) at n = 1024.  They cover the tiles whose inputs lie below offset
+// 2n-1; the generic kernel continues from the end of those tiles.
+int bdrt_fast_tiles(i64 n);
+int bdrt_fast_width();
+int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
+int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
+
+static bool bwd_fast_eligible(i64 n, size_t elem) {
+  if (elem != 4 || n < 256 || n > 1024 || !is_pow2(n)) return false;
+  const TuneConfig tc = tune_lookup(ADRT_GB300_OP_BDRT, ADRT_GB300_F32, n);
+  return tc.use_fast != 0 && (tc.max_fused == 0 || tc.max_fused == 5);
+}
+
+// Pass plan: the fast path undoes forward stages 0..4 in its own last pass
+// (sizes[0] = 5) and the remaining L-5 in the first.
+static int plan_bwd(i64 n, size_t elem, int *sizes) {
+  if (bwd_fast_eligible(n, elem)) {
+    sizes[0] = 5;
+    sizes[1] = num_iters(n) - 5;
+    return 2;
+  }
+  return plan_passes_bwd(n, elem, sizes);
+}
+
+// Row stride of the bdrt buffers: 2n-1, padded to 8 elements on the fast
+// path (16-byte aligned rows for its vector loads and stores).
+static i64 bwd_cs(i64 n, size_t elem) {
+  const i64 C = 2 * n - 1;
+  return bwd_fast_eligible(n, elem) ? (C + 7) / 8 * 8 : C;
+}
+
 // Images per chunk.  One chunk's intermediate has a built-in budget of 1 GB
 // (bdrt at n = 1024, float32, 128 images: 9.9k img/s against 8.5k with
 // 48 MB chunks whose intermediate stays in L2: fewer launch tails), or the
 // tuned one; chunks are balanced.
 static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
-  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  const size_t per = (size_t)4 * n * bwd_cs(n, elem) * elem;
   const int mb = tune_lookup(ADRT_GB300_OP_BDRT, elem == 4 ? ADRT_GB300_F32 : ADRT_GB300_F64, n).chunk_mb;
   const size_t budget = (size_t)(mb > 0 ? mb : 1024) << 20;
   i64 k = (i64)(budget / per);
@@ -252,9 +291,9 @@ static i64 bwd_chunk(i64 batch, i64 n, size_t elem) {
 
 size_t bwd_workspace_bytes(i64 batch, i64 n, size_t elem) {
   int sizes[16];
-  const int P = plan_passes_bwd(n, elem, sizes);
+  const int P = plan_bwd(n, elem, sizes);
   if (P <= 1) return 0;
-  const size_t per = (size_t)4 * n * (2 * n - 1) * elem;
+  const size_t per = (size_t)4 * n * bwd_cs(n, elem) * elem;
   return per * (P >= 3 ? 2 : 1) * (size_t)bwd_chunk(batch, n, elem);
 }
 
@@ -269,8 +308,10 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   // The pass kernels index one quadrant (n (2n-1) elements) in 32 bits.
   if (n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
   int sizes[16];
-  const int P = plan_passes_bwd(n, sizeof(T), sizes);
-  const size_t per = (size_t)4 * n * (2 * n - 1) * sizeof(T);
+  const int P = plan_bwd(n, sizeof(T), sizes);
+  const bool fast = bwd_fast_eligible(n, sizeof(T));
+  const i64 cs = bwd_cs(n, sizeof(T));
+  const size_t per = (size_t)4 * n * cs * sizeof(T);
   const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
   i64 chunk = bwd_chunk(batch, n, sizeof(T));
   if (nbuf) {
@@ -294,7 +335,20 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
       const i64 C = 2 * n - 1;
       const i64 need = rows_needed + (i64(1) << kstart[p]) - 1;
       BwdPassArgs a{src, dst, n, kstart[p], nb, need < C ? need : C};
-      int rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
+      a.cs = cs;
+      int rc = ADRT_GB300_OK;
+      if constexpr (sizeof(T) == 4) {
+        // Register-level tiles first; the generic kernel takes the rest.
+        if (fast && (last || n == 1024)) {
+          rc = last ? bdrt_fast_pass2(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,
+                                      a.c_need, st)
+                    : bdrt_fast_pass1(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,
+                                      a.c_need, st);
+          if (rc) return rc;
+          a.c_begin = bdrt_fast_tiles(n) * bdrt_fast_width();
+        }
+      }
+      rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
       if (rc) return rc;
       src = dst;
     }

@@ -1,0 +1,379 @@
+// Register-level bdrt passes for float32 (the transpose of the fast forward's
+// five-stage pass structure).
+//
+// The generic pass (bdrt.cu) holds a tile of 32 rows in shared memory and
+// runs each transposed stage through it.  Here a pass's five stages run in
+// registers, for the tiles where none of the reference's copy/zero rules
+// applies.  Inside a tile every row is kept in the tile frame (the pass's
+// pre-shift a' * i is applied only when member i is stored), so an undone
+// stage at local output angle li is
+//     left  [u] = A[u] + B[u]
+//     right [u] = A[u + li] + B[u + li + 1]
+// with A, B the rows of local angles 2 li and 2 li + 1 (src/adrt/
+// adrt_cdefs_bdrt.hpp:56-116).  The rules only act at reference offset 2n-2
+// and beyond: a tile whose input positions all lie below 2n-1 computes every
+// output with these two formulas, bit for bit like the reference; the tiles
+// past that point stay with the generic kernel.
+//
+//  group 2t (stages 4, 3, 2 undone): a lane holds the 8 angles 8 L1 + l3 at 8
+//    consecutive positions (block b); operands to the right come from lane+1
+//    by shuffle.  The L1-dependent part of the shifts (4 L1, 2 L1, L1) is left
+//    out, so level-2 combo h comes out L1 * h positions to the right of its
+//    tile position; the exchange write puts it back.
+//  exchange: level-2 rows (combo h, angle L1) in shared memory, 16-byte chunks
+//    XOR-swizzled as in the forward kernel.
+//  group 1t (stages 1, 0 undone): a warp owns combo h, a lane one 4-position
+//    chunk of its 4 angle rows; it produces members 4h..4h+3.
+//
+// The last lane of a warp cannot see its right neighbour, so it only seeds
+// lane 30: group-2t warps cover blocks 0..31 and 30..61, group-1t warps take
+// 31 chunks per sweep.
+#include "common.cuh"
+
+namespace adrtg {
+namespace bfast {
+
+constexpr int W = 448;             // stored tile positions per CTA (56 blocks of 8)
+constexpr int TWI = 496;           // input positions per tile (62 blocks)
+constexpr int NT = 256;
+constexpr int NCH = 128;           // exchange chunks per row
+constexpr int RS = 4 * (NCH + 1);  // exchange row stride in floats (odd chunk count)
+constexpr size_t SMEM = sizeof(float) * 32 * RS;
+constexpr unsigned FULL = 0xffffffffu;
+static_assert(TWI * 32 <= 32 * RS && W * 32 <= 32 * RS, "stagings fit in the exchange buffer");
+
+__device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
+
+__device__ __forceinline__ float4 ld4_cs(const float *p) { return __ldcs(reinterpret_cast<const float4 *>(p)); }
+
+// Right output of one undone stage over 8 positions: d[k] = A[k + s] +
+// B[k + s + 1], where positions 8.. come from lane + 1.
+template <int S>
+__device__ __forceinline__ void right8(const float (&A)[8], const float (&B)[8], float (&d)[8]) {
+  float ea[S > 0 ? S : 1], eb[S + 1];
+#pragma unroll
+  for (int k = 0; k < S; ++k) ea[k] = __shfl_down_sync(FULL, A[k], 1);
+#pragma unroll
+  for (int k = 0; k <= S; ++k) eb[k] = __shfl_down_sync(FULL, B[k], 1);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float a = k + S < 8 ? A[(k + S) & 7] : ea[(k + S - 8) & (S > 0 ? 7 : 0)];
+    const float b = k + S + 1 < 8 ? B[(k + S + 1) & 7] : eb[k + S + 1 - 8];
+    d[k] = add_rn(a, b);
+  }
+}
+
+__device__ __forceinline__ void left8(const float (&A)[8], const float (&B)[8], float (&d)[8]) {
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) add_rn2(A[k], A[k + 1], B[k], B[k + 1], d[k], d[k + 1]);
+}
+
+// Group 2t: a[l3] = angle 8 L1 + l3 at the lane's 8 positions -> t2[h] =
+// level-2 combo h (undone stages 4, 3, 2 give its bits, first as MSB).
+__device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8]) {
+  float t4[2][4][8];
+  left8(a[0], a[1], t4[0][0]);
+  right8<0>(a[0], a[1], t4[1][0]);
+  left8(a[2], a[3], t4[0][1]);
+  right8<1>(a[2], a[3], t4[1][1]);
+  left8(a[4], a[5], t4[0][2]);
+  right8<2>(a[4], a[5], t4[1][2]);
+  left8(a[6], a[7], t4[0][3]);
+  right8<3>(a[6], a[7], t4[1][3]);
+  float t3[2][2][2][8];
+#pragma unroll
+  for (int c4 = 0; c4 < 2; ++c4) {
+    left8(t4[c4][0], t4[c4][1], t3[c4][0][0]);
+    right8<0>(t4[c4][0], t4[c4][1], t3[c4][1][0]);
+    left8(t4[c4][2], t4[c4][3], t3[c4][0][1]);
+    right8<1>(t4[c4][2], t4[c4][3], t3[c4][1][1]);
+  }
+#pragma unroll
+  for (int c4 = 0; c4 < 2; ++c4)
+#pragma unroll
+    for (int c3 = 0; c3 < 2; ++c3) {
+      left8(t3[c4][c3][0], t3[c4][c3][1], t2[4 * c4 + 2 * c3]);
+      right8<0>(t3[c4][c3][0], t3[c4][c3][1], t2[4 * c4 + 2 * c3 + 1]);
+    }
+}
+
+// Writes combo h of angle L1 back to its tile positions: fresh position
+// 8b + k is tile position 8b + k - L1 h.  Lanes 30 and 31 write nothing (31
+// is a seed, 30's second chunk would need 31's values; the other half of the
+// CTA covers those blocks).
+template <int L1>
+__device__ __forceinline__ void put_exchange_t(float *xs, int b, bool wr, const float (&t2)[8][8]) {
+#pragma unroll
+  for (int h = 0; h < 8; ++h) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int sh = L1 * h, qh = sh >> 2, mh = sh & 3;
+    float nx[4];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (k < mh) nx[k] = __shfl_down_sync(FULL, t2[h][k], 1);
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = k + mh < 8 ? t2[h][(k + mh) & 7] : nx[(k + mh - 8) & 3];
+    if (wr) {
+      float *row = xs + (h * 4 + L1) * RS;
+      const int x0 = 2 * b - qh;
+      if (x0 >= 0) *reinterpret_cast<float4 *>(row + swz(x0) * 4) = make_float4(v[0], v[1], v[2], v[3]);
+      if (x0 + 1 >= 0) *reinterpret_cast<float4 *>(row + swz(x0 + 1) * 4) = make_float4(v[4], v[5], v[6], v[7]);
+    }
+  }
+}
+
+// Group-2t lane: warp w takes angle group L1 = w & 3; half w >> 2 covers
+// blocks 0..31 or 30..61.
+__device__ __forceinline__ int g2_block() {
+  const int lane = threadIdx.x & 31;
+  return (threadIdx.x >> 7) ? 30 + lane : lane;
+}
+
+template <int L1>
+__device__ __forceinline__ void group2t_and_exchange(float (&a)[8][8], float *xs) {
+  float t2[8][8];
+  group2t(a, t2);
+  const int lane = threadIdx.x & 31;
+  put_exchange_t<L1>(xs, g2_block(), lane < 30, t2);
+}
+
+// Group 1t for one sweep: chunk ch of combo h's four angle rows -> members
+// 4h + m at the chunk's positions, o[m][k].
+__device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&o)[4][4]) {
+  float x[4][4];
+#pragma unroll
+  for (int l1 = 0; l1 < 4; ++l1) {
+    const float4 v = *reinterpret_cast<const float4 *>(xs + (h * 4 + l1) * RS + swz(ch) * 4);
+    x[l1][0] = v.x; x[l1][1] = v.y; x[l1][2] = v.z; x[l1][3] = v.w;
+  }
+  const float n10 = __shfl_down_sync(FULL, x[1][0], 1);
+  const float n20 = __shfl_down_sync(FULL, x[2][0], 1);
+  const float n30 = __shfl_down_sync(FULL, x[3][0], 1);
+  const float n31 = __shfl_down_sync(FULL, x[3][1], 1);
+  // undo stage 1: u[side][li][k]
+  float u[2][2][5];
+  add_rn2(x[0][0], x[0][1], x[1][0], x[1][1], u[0][0][0], u[0][0][1]);
+  add_rn2(x[0][2], x[0][3], x[1][2], x[1][3], u[0][0][2], u[0][0][3]);
+  add_rn2(x[2][0], x[2][1], x[3][0], x[3][1], u[0][1][0], u[0][1][1]);
+  add_rn2(x[2][2], x[2][3], x[3][2], x[3][3], u[0][1][2], u[0][1][3]);
+  u[0][1][4] = add_rn(n20, n30);
+  const float x1e[5] = {x[1][0], x[1][1], x[1][2], x[1][3], n10};
+  const float x2e[5] = {x[2][0], x[2][1], x[2][2], x[2][3], n20};
+  const float x3e[6] = {x[3][0], x[3][1], x[3][2], x[3][3], n30, n31};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    u[1][0][k] = add_rn(x[0][k], x1e[k + 1]);
+    u[1][1][k] = add_rn(x2e[k + 1], x3e[k + 2]);
+  }
+  u[1][1][4] = __shfl_down_sync(FULL, u[1][1][0], 1);
+  // undo stage 0: member 4h + 2 side + s0
+#pragma unroll
+  for (int c1 = 0; c1 < 2; ++c1) {
+    add_rn2(u[c1][0][0], u[c1][0][1], u[c1][1][0], u[c1][1][1], o[2 * c1][0], o[2 * c1][1]);
+    add_rn2(u[c1][0][2], u[c1][0][3], u[c1][1][2], u[c1][1][3], o[2 * c1][2], o[2 * c1][3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[2 * c1 + 1][k] = add_rn(u[c1][0][k], u[c1][1][k + 1]);
+  }
+}
+
+// ---- pass 1 (forward stages 5..9 undone, n = 1024) ------------------------
+// Input: the (4, 2n-1, n) array, angles 32 a' .. 32 a' + 31 (128 bytes per
+// offset); output: bdrt buffer rows (a', member i) at reference offset
+// u - a' i, row stride cs.  A4 = a' mod 4 fixes each member's sub-chunk shift.
+template <int A4>
+__device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *rows_ap, int ap, int c0, int cs,
+                                            int C, int h) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int ch = 31 * it + lane;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      constexpr int dummy = 0;
+      (void)dummy;
+      const int i = 4 * h + m;
+      const int D = ap * i;
+      const int mi = (A4 * m) & 3;  // == D & 3
+      // The chunk to the right: lane + 1's, except for lane 30, whose right
+      // neighbour (lane 31) only seeds; that chunk is lane 0's next sweep.
+      float nx[4];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < mi) {
+          const float va = __shfl_sync(FULL, o[it][m][k], (lane + 1) & 31);
+          const float vb = it < 3 ? __shfl_sync(FULL, o[it < 3 ? it + 1 : it][m][k], 0) : va;
+          nx[k] = lane == 30 ? vb : va;
+        }
+      float v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = k + mi < 4 ? o[it][m][(k + mi) & 3] : nx[(k + mi - 4) & 3];
+      const int X = ch + (c0 >> 2) - (D >> 2);
+      if (lane < 31 && 4 * ch + mi < W && X >= 0 && 4 * X < C)
+        *reinterpret_cast<float4 *>(rows_ap + (size_t)i * cs + 4 * X) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ in, float *__restrict__ buf, int n,
+                                                      int cs, int need) {
+  extern __shared__ __align__(16) float xs[];
+  const int C = 2 * n - 1;
+  const int c0 = (int)blockIdx.x * W;
+  const int bq = (int)blockIdx.y;  // image * 4 + quadrant
+  const int ap = (int)blockIdx.z;
+  // Member i stores reference offsets >= c0 - 31 a': nothing needed here.
+  if (c0 >= need + 31 * ap) return;
+  const float *src = in + (size_t)bq * C * n + 32 * ap;
+  // Stage the tile's 496 offsets x 32 angles (128-byte rows), chunk j of row
+  // r at swizzled chunk j ^ ((r >> 3) & 7).
+  {
+    const int r0 = threadIdx.x >> 3, j = threadIdx.x & 7;
+    float4 v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int r = r0 + 32 * i;
+      if (r < TWI) v[i] = ld4_cs(src + (size_t)(c0 + r) * n + 4 * j);
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int r = r0 + 32 * i;
+      if (r < TWI) *reinterpret_cast<float4 *>(xs + r * 32 + 4 * (j ^ ((r >> 3) & 7))) = v[i];
+    }
+  }
+  __syncthreads();
+  const int L1 = (threadIdx.x >> 5) & 3, b = g2_block();
+  float a[8][8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int r = 8 * b + k, sw = b & 7;
+    const float4 v0 = *reinterpret_cast<const float4 *>(xs + r * 32 + 4 * ((2 * L1) ^ sw));
+    const float4 v1 = *reinterpret_cast<const float4 *>(xs + r * 32 + 4 * ((2 * L1 + 1) ^ sw));
+    a[0][k] = v0.x; a[1][k] = v0.y; a[2][k] = v0.z; a[3][k] = v0.w;
+    a[4][k] = v1.x; a[5][k] = v1.y; a[6][k] = v1.z; a[7][k] = v1.w;
+  }
+  __syncthreads();  // the exchange overlays the staging
+  switch (L1) {
+    case 0: group2t_and_exchange<0>(a, xs); break;
+    case 1: group2t_and_exchange<1>(a, xs); break;
+    case 2: group2t_and_exchange<2>(a, xs); break;
+    default: group2t_and_exchange<3>(a, xs); break;
+  }
+  __syncthreads();
+  const int h = threadIdx.x >> 5;
+  float o[4][4][4];
+#pragma unroll
+  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + (threadIdx.x & 31), o[it]);
+  float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * cs;
+  switch (ap & 3) {
+    case 0: pass1_store<0>(o, rows_ap, ap, c0, cs, C, h); break;
+    case 1: pass1_store<1>(o, rows_ap, ap, c0, cs, C, h); break;
+    case 2: pass1_store<2>(o, rows_ap, ap, c0, cs, C, h); break;
+    default: pass1_store<3>(o, rows_ap, ap, c0, cs, C, h); break;
+  }
+}
+
+// ---- pass 2 (forward stages 0..4 undone, any n >= 256) ---------------------
+// Input: bdrt buffer rows (angle l, section r) for l < 32, row stride cs;
+// output: (4, 2n-1, n) sections 32 r .. 32 r + 31 (128 bytes per offset),
+// staged in shared memory (chunk h of row p at chunk h ^ ((p >> 2) & 7)).
+__global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ buf, float *__restrict__ out, int n,
+                                                      int cs, int need) {
+  extern __shared__ __align__(16) float xs[];
+  const int C = 2 * n - 1;
+  const int c0 = (int)blockIdx.x * W;
+  if (c0 >= need) return;
+  const int bq = (int)blockIdx.y;
+  const int r = (int)blockIdx.z;
+  const int R = n / 32;  // sections per angle row group
+  const int L1 = (threadIdx.x >> 5) & 3, b = g2_block();
+  const float *src = buf + (size_t)bq * n * cs + ((size_t)(8 * L1) * R + r) * cs + c0 + 8 * b;
+  float a[8][8];
+#pragma unroll
+  for (int l3 = 0; l3 < 8; ++l3) {
+    const float *p = src + (size_t)l3 * R * cs;
+    const float4 v0 = ld4_cs(p), v1 = ld4_cs(p + 4);
+    a[l3][0] = v0.x; a[l3][1] = v0.y; a[l3][2] = v0.z; a[l3][3] = v0.w;
+    a[l3][4] = v1.x; a[l3][5] = v1.y; a[l3][6] = v1.z; a[l3][7] = v1.w;
+  }
+  switch (L1) {
+    case 0: group2t_and_exchange<0>(a, xs); break;
+    case 1: group2t_and_exchange<1>(a, xs); break;
+    case 2: group2t_and_exchange<2>(a, xs); break;
+    default: group2t_and_exchange<3>(a, xs); break;
+  }
+  __syncthreads();
+  const int h = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float o[4][4][4];
+#pragma unroll
+  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + lane, o[it]);
+  __syncthreads();  // the output staging overlays the exchange
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int ch = 31 * it + lane;
+    if (lane < 31 && ch < W / 4) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int p = 4 * ch + k;
+        *reinterpret_cast<float4 *>(xs + p * 32 + 4 * (h ^ (ch & 7))) =
+            make_float4(o[it][0][k], o[it][1][k], o[it][2][k], o[it][3][k]);
+      }
+    }
+  }
+  __syncthreads();
+  const int p0 = threadIdx.x >> 3, j = threadIdx.x & 7;
+  float *dst = out + (size_t)bq * C * n + 32 * r + 4 * j;
+  const int lim = min(min(C, need) - c0, W);
+#pragma unroll
+  for (int i = 0; i < W / 32; ++i) {
+    const int p = p0 + 32 * i;
+    if (p < lim) {
+      const float4 v = *reinterpret_cast<const float4 *>(xs + p * 32 + 4 * (j ^ ((p >> 2) & 7)));
+      __stcs(reinterpret_cast<float4 *>(dst + (size_t)(c0 + p) * n), v);
+    }
+  }
+}
+
+}  // namespace bfast
+
+// Tiles of the register-level passes: those whose input offsets all lie below
+// 2n-1 (c0 + 496 <= 2n-1); the generic kernel continues from their end.
+int bdrt_fast_tiles(i64 n) {
+  const i64 C = 2 * n - 1;
+  return C >= bfast::TWI ? (int)((C - bfast::TWI) / bfast::W + 1) : 0;
+}
+int bdrt_fast_width() { return bfast::W; }
+
+int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+  static std::atomic<unsigned long long> configured{0};
+  if (const int rc = smem_limit_once((const void *)bfast::pass1_kernel, bfast::SMEM, configured)) return rc;
+  const int tiles = bdrt_fast_tiles(n);
+  if (tiles == 0 || n != 1024) return ADRT_GB300_ERR_SHAPE;
+  // Grid y counts (image, quadrant) pairs: launches of at most 16383 images.
+  for (i64 b0 = 0; b0 < batch; b0 += 16383) {
+    const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
+    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), 32);
+    bfast::pass1_kernel<<<grid, bfast::NT, bfast::SMEM, st>>>(in + b0 * 4 * (2 * n - 1) * n, buf + b0 * 4 * n * cs,
+                                                                (int)n, (int)cs, (int)need);
+    if (const int rc = launch_status()) return rc;
+  }
+  return ADRT_GB300_OK;
+}
+
+int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+  static std::atomic<unsigned long long> configured{0};
+  if (const int rc = smem_limit_once((const void *)bfast::pass2_kernel, bfast::SMEM, configured)) return rc;
+  const int tiles = bdrt_fast_tiles(n);
+  if (tiles == 0 || n < 256 || n > 1024) return ADRT_GB300_ERR_SHAPE;
+  for (i64 b0 = 0; b0 < batch; b0 += 16383) {
+    const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
+    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(n / 32));
+    bfast::pass2_kernel<<<grid, bfast::NT, bfast::SMEM, st>>>(buf + b0 * 4 * n * cs, out + b0 * 4 * (2 * n - 1) * n,
+                                                                (int)n, (int)cs, (int)need);
+    if (const int rc = launch_status()) return rc;
+  }
+  return ADRT_GB300_OK;
+}
+
+}  // namespace adrtg

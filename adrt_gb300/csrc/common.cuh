@@ -26,6 +26,17 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+// Two float32 adds in one packed instruction: d0 = a0 + b0, d1 = a1 + b1,
+// each rounded to nearest like add_rn (add.rn.f32x2 rounds per element).
+// Used where both operands of two neighbouring positions are adjacent in
+// registers (butterfly shifts that are even).
+__device__ __forceinline__ void add_rn2(float a0, float a1, float b0, float b1, float &d0, float &d1) {
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d0), "=f"(d1)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 // Fused multiply-add, for kernels whose results are not compared bit for bit
 // with the reference (the CG preconditioner).
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
