@@ -40,7 +40,6 @@ struct BwdPassArgs {
   i64 batch;
   i64 c_need;      // pass outputs are needed at reference offsets < c_need
   i64 cs = 0;      // row stride of the bdrt buffers (0: 2n-1)
-  int c_begin = 0; // first tile position of this launch (tiles before it are done elsewhere)
 };
 
 // Buffer layout between passes, per (b, q): [angle s][section p][offset c],
@@ -66,11 +65,10 @@ struct BwdTile {
 
 // Column tiles of one pass: tile positions span [0, C + a'_max * (2^S - 1)) so
 // every member's pre-shifted window is covered.
-static __host__ __device__ inline int bwd_col_tiles(i64 n, int k0, int S, int W, int c_begin = 0) {
+static __host__ __device__ inline int bwd_col_tiles(i64 n, int k0, int S, int W) {
   const i64 C = 2 * n - 1;
   const i64 max_ext = ((i64(1) << k0) - 1) * ((1 << S) - 1);
-  const i64 span = C + max_ext - c_begin;
-  return span > 0 ? (int)((span + W - 1) / W) : 0;
+  return (int)((C + max_ext + W - 1) / W);
 }
 
 // Per-quadrant index arithmetic is 32-bit: a quadrant holds n (2n-1) < 2^32
@@ -91,7 +89,7 @@ bwd_pass_kernel(BwdPassArgs args) {
   const unsigned A_lo = 1u << k0;      // angles after this pass (pass output)
   const unsigned R_lo = n >> k0;       // sections after this pass
   const unsigned R_hi = R_lo >> S;     // sections at pass input
-  const int col_tiles = bwd_col_tiles(args.n, k0, S, W, args.c_begin);
+  const int col_tiles = bwd_col_tiles(args.n, k0, S, W);
   const unsigned cs = args.cs ? (unsigned)args.cs : (unsigned)C;  // bdrt buffer row stride
 
   unsigned t = blockIdx.x;
@@ -100,7 +98,7 @@ bwd_pass_kernel(BwdPassArgs args) {
   const unsigned r = t % R_hi; t /= R_hi;
   const unsigned q = t & 3u; t >>= 2;
   const unsigned b = t;
-  const int c0 = args.c_begin + ct * W;
+  const int c0 = ct * W;
   // Skip tiles that hold no member's needed offsets (member i of this tile
   // stores reference offsets >= c0 - a'*i).
   if ((i64)c0 >= args.c_need + (i64)ap * (ROWS - 1)) return;
@@ -213,9 +211,8 @@ static int launch_bwd_pass(const BwdPassArgs &a, cudaStream_t st) {
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
   const i64 A_lo = i64(1) << a.k0;
-  const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W, a.c_begin);
+  const i64 col_tiles = bwd_col_tiles(a.n, a.k0, S, BwdTile<T, ROWS, NT>::W);
   const i64 tiles = a.batch * 4 * ((a.n >> a.k0) >> S) * A_lo * col_tiles;
-  if (tiles == 0) return ADRT_GB300_OK;
   kern<<<(unsigned)tiles, NT, smem, st>>>(a);
   return launch_status();
 }
@@ -243,10 +240,7 @@ static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cuda
 
 // Register-level passes (bdrt_fast.cu), float32, 256 <= n <= 1024: the last
 // bdrt pass (forward stages 0..4) for every such n, the first one (stages
-// 5..9) at n = 1024.  They cover the tiles whose inputs lie below offset
-// 2n-1; the generic kernel continues from the end of those tiles.
-int bdrt_fast_tiles(i64 n);
-int bdrt_fast_width();
+// 5..9) at n = 1024.
 int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
 int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
 
@@ -337,18 +331,17 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
       BwdPassArgs a{src, dst, n, kstart[p], nb, need < C ? need : C};
       a.cs = cs;
       int rc = ADRT_GB300_OK;
+      bool done = false;
       if constexpr (sizeof(T) == 4) {
-        // Register-level tiles first; the generic kernel takes the rest.
         if (fast && (last || n == 1024)) {
           rc = last ? bdrt_fast_pass2(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,
                                       a.c_need, st)
                     : bdrt_fast_pass1(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,
                                       a.c_need, st);
-          if (rc) return rc;
-          a.c_begin = bdrt_fast_tiles(n) * bdrt_fast_width();
+          done = true;
         }
       }
-      rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
+      if (!done) rc = bwd_dispatch<T>(sizes[p], first, last, a, st);
       if (rc) return rc;
       src = dst;
     }

@@ -10,10 +10,15 @@
 //     left  [u] = A[u] + B[u]
 //     right [u] = A[u + li] + B[u + li + 1]
 // with A, B the rows of local angles 2 li and 2 li + 1 (src/adrt/
-// adrt_cdefs_bdrt.hpp:56-116).  The rules only act at reference offset 2n-2
-// and beyond: a tile whose input positions all lie below 2n-1 computes every
-// output with these two formulas, bit for bit like the reference; the tiles
-// past that point stay with the generic kernel.
+// adrt_cdefs_bdrt.hpp:56-116).  The reference's copy and zero rules (right =
+// copy of A where B's offset is 2n-1, +0 beyond) are what these formulas give
+// when every row reads as +0 at reference offsets >= 2n-1, except a row used
+// as B, which must read -0 at exactly 2n-1 (A + (-0) == A bit for bit).  The
+// sums beyond 2n-1 come out +0 by themselves, so in tiles that reach that
+// offset ("edge" tiles) the inputs there are filled that way and, after each
+// undone stage, the one position of each B row at offset 2n-1 is set to -0.
+// Row (combo m, level J) sits at tile position u <-> reference offset
+// c0 + u - a' m 2^J; in group 2t's frame (below) also + L1 m 2^(J-2).
 //
 //  group 2t (stages 4, 3, 2 undone): a lane holds the 8 angles 8 L1 + l3 at 8
 //    consecutive positions (block b); operands to the right come from lane+1
@@ -68,9 +73,21 @@ __device__ __forceinline__ void left8(const float (&A)[8], const float (&B)[8], 
   for (int k = 0; k < 8; k += 2) add_rn2(A[k], A[k + 1], B[k], B[k + 1], d[k], d[k + 1]);
 }
 
+// Sets v[f - base] to -0 when this lane holds position f.
+template <int K>
+__device__ __forceinline__ void neg0_at(float (&v)[K], int f_minus_base) {
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (f_minus_base == k) v[k] = -0.f;
+}
+
 // Group 2t: a[l3] = angle 8 L1 + l3 at the lane's 8 positions -> t2[h] =
-// level-2 combo h (undone stages 4, 3, 2 give its bits, first as MSB).
-__device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8]) {
+// level-2 combo h (undone stages 4, 3, 2 give its bits, first as MSB).  In
+// edge tiles (edge set) the B rows of levels 4 and 3 get their -0 at offset
+// 2n-1: fresh position kc + m (2^J a' + 2^(J-2) L1) for combo m at level J,
+// kc = 2n-1 - c0; base = 8 b.
+template <int L1>
+__device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8], bool edge, int kc, int ap, int base) {
   float t4[2][4][8];
   left8(a[0], a[1], t4[0][0]);
   right8<0>(a[0], a[1], t4[1][0]);
@@ -80,6 +97,14 @@ __device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8]) {
   right8<2>(a[4], a[5], t4[1][2]);
   left8(a[6], a[7], t4[0][3]);
   right8<3>(a[6], a[7], t4[1][3]);
+  if (edge) {
+#pragma unroll
+    for (int c4 = 0; c4 < 2; ++c4) {
+      const int f = kc + c4 * (16 * ap + 4 * L1) - base;
+      neg0_at(t4[c4][1], f);
+      neg0_at(t4[c4][3], f);
+    }
+  }
   float t3[2][2][2][8];
 #pragma unroll
   for (int c4 = 0; c4 < 2; ++c4) {
@@ -87,6 +112,12 @@ __device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8]) {
     right8<0>(t4[c4][0], t4[c4][1], t3[c4][1][0]);
     left8(t4[c4][2], t4[c4][3], t3[c4][0][1]);
     right8<1>(t4[c4][2], t4[c4][3], t3[c4][1][1]);
+  }
+  if (edge) {
+#pragma unroll
+    for (int c4 = 0; c4 < 2; ++c4)
+#pragma unroll
+      for (int c3 = 0; c3 < 2; ++c3) neg0_at(t3[c4][c3][1], kc + (2 * c4 + c3) * (8 * ap + 2 * L1) - base);
   }
 #pragma unroll
   for (int c4 = 0; c4 < 2; ++c4)
@@ -132,21 +163,30 @@ __device__ __forceinline__ int g2_block() {
 }
 
 template <int L1>
-__device__ __forceinline__ void group2t_and_exchange(float (&a)[8][8], float *xs) {
+__device__ __forceinline__ void group2t_and_exchange(float (&a)[8][8], float *xs, bool edge, int kc, int ap) {
   float t2[8][8];
-  group2t(a, t2);
+  const int b = g2_block();
+  group2t<L1>(a, t2, edge, kc, ap, 8 * b);
   const int lane = threadIdx.x & 31;
-  put_exchange_t<L1>(xs, g2_block(), lane < 30, t2);
+  put_exchange_t<L1>(xs, b, lane < 30, t2);
 }
 
 // Group 1t for one sweep: chunk ch of combo h's four angle rows -> members
 // 4h + m at the chunk's positions, o[m][k].
-__device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&o)[4][4]) {
+// Edge tiles: the B rows of level 2 (odd angles) and level 1 get -0 at tile
+// position kc + 4 a' h and kc + 2 a' (2h + c1).
+__device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&o)[4][4], bool edge, int kc,
+                                        int ap) {
   float x[4][4];
 #pragma unroll
   for (int l1 = 0; l1 < 4; ++l1) {
     const float4 v = *reinterpret_cast<const float4 *>(xs + (h * 4 + l1) * RS + swz(ch) * 4);
     x[l1][0] = v.x; x[l1][1] = v.y; x[l1][2] = v.z; x[l1][3] = v.w;
+  }
+  if (edge) {
+    const int f = kc + 4 * ap * h - 4 * ch;
+    neg0_at(x[1], f);
+    neg0_at(x[3], f);
   }
   const float n10 = __shfl_down_sync(FULL, x[1][0], 1);
   const float n20 = __shfl_down_sync(FULL, x[2][0], 1);
@@ -166,6 +206,13 @@ __device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&
   for (int k = 0; k < 4; ++k) {
     u[1][0][k] = add_rn(x[0][k], x1e[k + 1]);
     u[1][1][k] = add_rn(x2e[k + 1], x3e[k + 2]);
+  }
+  if (edge) {
+    neg0_at(u[0][1], kc + 4 * ap * h - 4 * ch);  // positions 0..4 (4: next chunk's first)
+    float t[4] = {u[1][1][0], u[1][1][1], u[1][1][2], u[1][1][3]};
+    neg0_at(t, kc + 2 * ap * (2 * h + 1) - 4 * ch);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[1][1][k] = t[k];
   }
   u[1][1][4] = __shfl_down_sync(FULL, u[1][1][0], 1);
   // undo stage 0: member 4h + 2 side + s0
@@ -225,16 +272,22 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
   const int ap = (int)blockIdx.z;
   // Member i stores reference offsets >= c0 - 31 a': nothing needed here.
   if (c0 >= need + 31 * ap) return;
+  const int kc = C - c0;
+  const bool edge = kc < TWI;
   const float *src = in + (size_t)bq * C * n + 32 * ap;
   // Stage the tile's 496 offsets x 32 angles (128-byte rows), chunk j of row
-  // r at swizzled chunk j ^ ((r >> 3) & 7).
+  // r at swizzled chunk j ^ ((r >> 3) & 7).  Offsets >= 2n-1 read +0, and
+  // -0 for the odd angles (B rows) at 2n-1 itself.
   {
     const int r0 = threadIdx.x >> 3, j = threadIdx.x & 7;
     float4 v[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
       const int r = r0 + 32 * i;
-      if (r < TWI) v[i] = ld4_cs(src + (size_t)(c0 + r) * n + 4 * j);
+      if (r < TWI) {
+        if (r < kc) v[i] = ld4_cs(src + (size_t)(c0 + r) * n + 4 * j);
+        else v[i] = r == kc ? make_float4(0.f, -0.f, 0.f, -0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
     }
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -255,16 +308,16 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
   }
   __syncthreads();  // the exchange overlays the staging
   switch (L1) {
-    case 0: group2t_and_exchange<0>(a, xs); break;
-    case 1: group2t_and_exchange<1>(a, xs); break;
-    case 2: group2t_and_exchange<2>(a, xs); break;
-    default: group2t_and_exchange<3>(a, xs); break;
+    case 0: group2t_and_exchange<0>(a, xs, edge, kc, ap); break;
+    case 1: group2t_and_exchange<1>(a, xs, edge, kc, ap); break;
+    case 2: group2t_and_exchange<2>(a, xs, edge, kc, ap); break;
+    default: group2t_and_exchange<3>(a, xs, edge, kc, ap); break;
   }
   __syncthreads();
   const int h = threadIdx.x >> 5;
   float o[4][4][4];
 #pragma unroll
-  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + (threadIdx.x & 31), o[it]);
+  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + (threadIdx.x & 31), o[it], edge, kc, ap);
   float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * cs;
   switch (ap & 3) {
     case 0: pass1_store<0>(o, rows_ap, ap, c0, cs, C, h); break;
@@ -288,26 +341,41 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
   const int r = (int)blockIdx.z;
   const int R = n / 32;  // sections per angle row group
   const int L1 = (threadIdx.x >> 5) & 3, b = g2_block();
-  const float *src = buf + (size_t)bq * n * cs + ((size_t)(8 * L1) * R + r) * cs + c0 + 8 * b;
+  const int kc = C - c0;
+  const bool edge = kc < TWI;
+  const int e0 = 8 * b;  // lane's first tile position
+  const float *src = buf + (size_t)bq * n * cs + ((size_t)(8 * L1) * R + r) * cs + c0 + e0;
+  // Chunks that start at or past 2n-1 read +0 without a memory access (the
+  // last chunk of a row ends exactly at 2n-1); offset 2n-1 itself is set
+  // below: -0 on the odd angles (B rows), +0 on the even ones.
   float a[8][8];
 #pragma unroll
   for (int l3 = 0; l3 < 8; ++l3) {
     const float *p = src + (size_t)l3 * R * cs;
-    const float4 v0 = ld4_cs(p), v1 = ld4_cs(p + 4);
+    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+    if (e0 < kc) v0 = ld4_cs(p);
+    if (e0 + 4 < kc) v1 = ld4_cs(p + 4);
     a[l3][0] = v0.x; a[l3][1] = v0.y; a[l3][2] = v0.z; a[l3][3] = v0.w;
     a[l3][4] = v1.x; a[l3][5] = v1.y; a[l3][6] = v1.z; a[l3][7] = v1.w;
   }
+  if (edge) {
+#pragma unroll
+    for (int l3 = 0; l3 < 8; ++l3)
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (e0 + k == kc) a[l3][k] = (l3 & 1) ? -0.f : 0.f;
+  }
   switch (L1) {
-    case 0: group2t_and_exchange<0>(a, xs); break;
-    case 1: group2t_and_exchange<1>(a, xs); break;
-    case 2: group2t_and_exchange<2>(a, xs); break;
-    default: group2t_and_exchange<3>(a, xs); break;
+    case 0: group2t_and_exchange<0>(a, xs, edge, kc, 0); break;
+    case 1: group2t_and_exchange<1>(a, xs, edge, kc, 0); break;
+    case 2: group2t_and_exchange<2>(a, xs, edge, kc, 0); break;
+    default: group2t_and_exchange<3>(a, xs, edge, kc, 0); break;
   }
   __syncthreads();
   const int h = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float o[4][4][4];
 #pragma unroll
-  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + lane, o[it]);
+  for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + lane, o[it], edge, kc, 0);
   __syncthreads();  // the output staging overlays the exchange
 #pragma unroll
   for (int it = 0; it < 4; ++it) {
@@ -337,19 +405,19 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
 
 }  // namespace bfast
 
-// Tiles of the register-level passes: those whose input offsets all lie below
-// 2n-1 (c0 + 496 <= 2n-1); the generic kernel continues from their end.
-int bdrt_fast_tiles(i64 n) {
-  const i64 C = 2 * n - 1;
-  return C >= bfast::TWI ? (int)((C - bfast::TWI) / bfast::W + 1) : 0;
+// Column tiles: pass 2 covers offsets [0, 2n-1); pass 1 tile positions
+// [0, 2n-1 + 31 * 31) (member i of input angle group a' is stored 31 a'
+// positions to the left at most).
+static int pass_tiles(i64 n, bool first) {
+  const i64 span = 2 * n - 1 + (first ? 31 * 31 : 0);
+  return (int)((span + bfast::W - 1) / bfast::W);
 }
-int bdrt_fast_width() { return bfast::W; }
 
 int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)bfast::pass1_kernel, bfast::SMEM, configured)) return rc;
-  const int tiles = bdrt_fast_tiles(n);
-  if (tiles == 0 || n != 1024) return ADRT_GB300_ERR_SHAPE;
+  const int tiles = pass_tiles(n, true);
+  if (n != 1024) return ADRT_GB300_ERR_SHAPE;
   // Grid y counts (image, quadrant) pairs: launches of at most 16383 images.
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
@@ -364,8 +432,8 @@ int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 n
 int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)bfast::pass2_kernel, bfast::SMEM, configured)) return rc;
-  const int tiles = bdrt_fast_tiles(n);
-  if (tiles == 0 || n < 256 || n > 1024) return ADRT_GB300_ERR_SHAPE;
+  const int tiles = pass_tiles(n, false);
+  if (n < 256 || n > 1024) return ADRT_GB300_ERR_SHAPE;
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
     const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(n / 32));
