@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fwd_fast.cuh"
 #include "tune.cuh"
 
 namespace adrtg {
@@ -305,6 +306,7 @@ static i64 fwd_chunk(i64 batch, i64 n, size_t elem) {
 // Fast path for float32, 64 <= n <= 1024 (adrt_fwd_fast.cu).
 bool fast_forward_eligible(i64 n, size_t elem);
 size_t fast_workspace_bytes(i64 batch, i64 n);
+int fast_inter_cs(i64 n);
 int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                       cudaStream_t st);
 
@@ -335,7 +337,7 @@ template <typename T>
 int adrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                  cudaStream_t st) {
   if constexpr (sizeof(T) == 4) {
-    if (use_fast_path(n, sizeof(T)))
+    if (use_fast_path(n, sizeof(T)) && aligned32(in) && aligned32(out))
       return adrt_forward_fast(reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out),
                                batch, n, ws, ws_bytes, st);
   }
@@ -385,14 +387,25 @@ template int adrt_forward<double>(const double *, double *, i64, i64, void *, si
 // kernel raises the error word and stops taking work.
 // ---------------------------------------------------------------------------
 
+// Item kinds: a generic pass tile, or a tile of the fast float32 passes
+// (pass A at n = 1024; pass B for 64 <= n <= 1024, reading the padded
+// intermediate [q][32][n/32][cs] that pass A or a generic first pass wrote).
+enum { RAGGED_GENERIC = 0, RAGGED_FAST_A = 1, RAGGED_FAST_B = 2 };
+
 struct RaggedImage {
   i64 in_off, out_off, inter_off;  // element offsets in the packed buffers
   int n, s0, s1;                   // side, stages of pass 0 and pass 1 (0: none)
   int tiles0;                      // tiles of pass 0
+  int kind0, kind1;                // item kinds of pass 0 and pass 1
+  int cs;                          // intermediate row stride (0: 2n-1)
+  int pad;
 };
 
+// An item is `count` consecutive tiles of one pass of one image (small
+// generic tiles are grouped so that the per-item ticket and barriers are paid
+// on enough work).
 struct RaggedItem {
-  int image, pass, tile, pad;
+  int image, pass, tile, count;
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -412,6 +425,24 @@ __device__ __forceinline__ void ragged_tile_S(int S, const FwdPassArgs &a, i64 t
     case 4: fwd_tile<T, 4, FIRST, LAST, kFwdWNarrow>(a, tile, smem); break;
     default: fwd_tile<T, 5, FIRST, LAST, kFwdWNarrow>(a, tile, smem); break;
   }
+}
+
+// Item bodies of the ragged kernel, each kept out of line: inlined into one
+// loop, the generic and fast tiles' register needs add up and spill.
+template <typename T, bool FIRST, bool LAST>
+__device__ __noinline__ void ragged_generic_item(int S, const FwdPassArgs a, i64 tile, unsigned char *smem) {
+  ragged_tile_S<T, FIRST, LAST>(S, a, tile, smem);
+}
+
+__device__ __forceinline__ void ragged_fast_a_item(const float *img, float *inter_img, int t, float *xs) {
+  fast::pass_a_tile<true>(img, inter_img, t / (fast::A_TILES * 32), (t / fast::A_TILES) % 32, t % fast::A_TILES,
+                         xs);
+}
+
+__device__ __forceinline__ void ragged_fast_b_item(const float *inter_img, float *out_img, int n, int cs, int t,
+                                                float *xs) {
+  const int ctn = fast::pass_b_col_tiles(n);
+  fast::pass_b_tile<fast::LD_CG, true>(inter_img, out_img, n, cs, (t / ctn) % 4, t / (ctn * 4), t % ctn, xs);
 }
 
 // ctl[0]: next ticket, ctl[1]: error word.
@@ -436,8 +467,10 @@ ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__
       if (threadIdx.x == 0) {
         int ok = 1;
         const unsigned long long t0 = global_ns();
-        while (atomicAdd(&counters[item.image], 0u) < (unsigned)im.tiles0) {
-          if (atomicAdd(&ctl[1], 0u) != 0u || global_ns() - t0 > wait_ns) {
+        const volatile unsigned *done = counters + item.image;
+        const volatile unsigned *err = ctl + 1;
+        while (*done < (unsigned)im.tiles0) {
+          if (*err != 0u || global_ns() - t0 > wait_ns) {
             ok = 0;
             atomicExch(&ctl[1], 1u);
             break;
@@ -450,25 +483,46 @@ ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__
       __syncthreads();
       if (!s_ok) break;
     }
+    if constexpr (sizeof(T) == 4) {
+      float *xs = reinterpret_cast<float *>(smem_raw);
+      const int kind = item.pass == 0 ? im.kind0 : im.kind1;
+      if (kind == RAGGED_FAST_A)
+        ragged_fast_a_item(reinterpret_cast<const float *>(in) + im.in_off,
+                           reinterpret_cast<float *>(inter) + im.inter_off, item.tile, xs);
+      else if (kind == RAGGED_FAST_B)
+        ragged_fast_b_item(reinterpret_cast<const float *>(inter) + im.inter_off,
+                           reinterpret_cast<float *>(out) + im.out_off, im.n, im.cs, item.tile, xs);
+      if (kind != RAGGED_GENERIC) {
+        __syncthreads();
+        if (item.pass == 0 && im.s1 > 0 && threadIdx.x == 0) {
+          __threadfence();
+          atomicAdd(&counters[item.image], 1u);
+        }
+        continue;
+      }
+    }
     FwdPassArgs a;
     a.n = im.n;
     a.batch = 1;
-    a.cs_out = 0;
-    if (item.pass == 0) {
-      a.in = in + im.in_off;
-      a.k0 = 0;
-      if (im.s1 == 0) {
-        a.out = out + im.out_off;
-        ragged_tile_S<T, true, true>(im.s0, a, item.tile, smem_raw);
+    a.cs_out = im.cs;
+    for (int t = item.tile; t < item.tile + item.count; ++t) {
+      if (t > item.tile) __syncthreads();  // the previous tile is done with shared memory
+      if (item.pass == 0) {
+        a.in = in + im.in_off;
+        a.k0 = 0;
+        if (im.s1 == 0) {
+          a.out = out + im.out_off;
+          ragged_generic_item<T, true, true>(im.s0, a, t, smem_raw);
+        } else {
+          a.out = inter + im.inter_off;
+          ragged_generic_item<T, true, false>(im.s0, a, t, smem_raw);
+        }
       } else {
-        a.out = inter + im.inter_off;
-        ragged_tile_S<T, true, false>(im.s0, a, item.tile, smem_raw);
+        a.in = inter + im.inter_off;
+        a.out = out + im.out_off;
+        a.k0 = im.s0;
+        ragged_generic_item<T, false, true>(im.s1, a, t, smem_raw);
       }
-    } else {
-      a.in = inter + im.inter_off;
-      a.out = out + im.out_off;
-      a.k0 = im.s0;
-      ragged_tile_S<T, false, true>(im.s1, a, item.tile, smem_raw);
     }
     __syncthreads();
     if (item.pass == 0 && im.s1 > 0 && threadIdx.x == 0) {
@@ -487,19 +541,83 @@ struct RaggedPlan {
 
 static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// Per-image plan of a ragged batch: passes, item kinds, tiles, intermediate.
+struct RaggedImagePlan {
+  int s0, s1, kind0, kind1, cs;
+  i64 tiles0, tiles1, inter_elems;
+};
+
+// Tiles per item: generic tiles of S stages hold 2^S rows x 160 positions;
+// they are grouped to about 16k elements per item.  Fast tiles: one each.
+static int ragged_group(int kind, int S) {
+  if (kind != RAGGED_GENERIC) return 1;
+  const int per = (1 << S) * (kFwdWNarrow + kFwdHalo);
+  const int g = 16384 / per;
+  return g < 1 ? 1 : g;
+}
+
+static i64 ragged_items(i64 tiles, int kind, int S) {
+  const int g = ragged_group(kind, S);
+  return (tiles + g - 1) / g;
+}
+
+static bool ragged_fast_size(i64 n, size_t elem) {
+  return elem == 4 && fast_forward_eligible(n, elem) && tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).use_fast != 0;
+}
+
+// fast: the image may use the fast tiles (its size allows it, and its input
+// and output are 32-byte aligned for their vector loads and stores).
+static RaggedImagePlan ragged_image_plan(i64 n, size_t elem, bool fast) {
+  RaggedImagePlan ip{};
+  const int L = num_iters(n);
+  if (fast && ragged_fast_size(n, elem)) {
+    ip.s0 = L - 5;
+    ip.s1 = 5;
+    ip.cs = fast_inter_cs(n);
+    ip.kind0 = n == fast::N ? RAGGED_FAST_A : RAGGED_GENERIC;
+    ip.kind1 = RAGGED_FAST_B;
+    ip.tiles0 = n == fast::N ? 4 * 32 * fast::A_TILES : fwd_pass_tiles(n, ip.s0, kFwdWNarrow);
+    ip.tiles1 = 4 * (n / 32) * fast::pass_b_col_tiles((int)n);
+    ip.inter_elems = 4 * n * ip.cs;
+    return ip;
+  }
+  int sz[16];
+  const int P = plan_passes(L, sz);
+  ip.s0 = sz[0];
+  ip.s1 = P == 2 ? sz[1] : 0;
+  ip.tiles0 = fwd_pass_tiles(n, ip.s0, kFwdWNarrow);
+  ip.tiles1 = P == 2 ? fwd_pass_tiles(n, ip.s1, kFwdWNarrow) : 0;
+  ip.inter_elems = P == 2 ? 4 * n * (2 * n - 1) : 0;
+  return ip;
+}
+
+// One image's slot in the intermediate buffer: room for either plan, a
+// multiple of 64 elements so that every slot starts 256-byte aligned.
+static i64 ragged_inter_slot(i64 n, size_t elem) {
+  i64 e = ragged_image_plan(n, elem, false).inter_elems;
+  if (ragged_fast_size(n, elem)) {
+    const i64 f = ragged_image_plan(n, elem, true).inter_elems;
+    if (f > e) e = f;
+  }
+  return (e + 63) / 64 * 64;
+}
+
+// Workspace layout from per-image upper bounds (the items and intermediate
+// of either plan), so that it does not depend on the buffers' alignment.
 static int ragged_plan(const int64_t *sizes, i64 count, size_t elem, RaggedPlan &p) {
   i64 items = 0, inter = 0;
   for (i64 i = 0; i < count; ++i) {
     const i64 n = sizes[i];
     if (n < 1 || !is_pow2(n) || n > 1024) return ADRT_GB300_ERR_SHAPE;
-    const int L = num_iters(n);
-    int sz[16];
-    const int P = plan_passes(L, sz);
-    items += fwd_pass_tiles(n, sz[0], kFwdWNarrow);
-    if (P == 2) {
-      items += fwd_pass_tiles(n, sz[1], kFwdWNarrow);
-      inter += 4 * n * (2 * n - 1);
+    const RaggedImagePlan g = ragged_image_plan(n, elem, false);
+    i64 it = ragged_items(g.tiles0, g.kind0, g.s0) + ragged_items(g.tiles1, g.kind1, g.s1);
+    if (ragged_fast_size(n, elem)) {
+      const RaggedImagePlan f = ragged_image_plan(n, elem, true);
+      const i64 fi = ragged_items(f.tiles0, f.kind0, f.s0) + ragged_items(f.tiles1, f.kind1, f.s1);
+      if (fi > it) it = fi;
     }
+    items += it;
+    inter += ragged_inter_slot(n, elem);
   }
   p.n_items = items;
   p.inter_elems = inter;
@@ -531,24 +649,29 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
   // Host-side descriptors.
   std::vector<RaggedImage> imgs((size_t)count);
   i64 in_off = 0, out_off = 0, inter_off = 0;
+  std::vector<RaggedImagePlan> plans((size_t)count);
   for (i64 i = 0; i < count; ++i) {
     const i64 n = sizes[i];
-    int sz[16];
-    const int P = plan_passes(num_iters(n), sz);
+    const bool fast = aligned32(in + in_off) && aligned32(out + out_off);
+    const RaggedImagePlan ip = plans[(size_t)i] = ragged_image_plan(n, sizeof(T), fast);
     RaggedImage &im = imgs[(size_t)i];
     im.in_off = in_off;
     im.out_off = out_off;
     im.inter_off = inter_off;
     im.n = (int)n;
-    im.s0 = sz[0];
-    im.s1 = P == 2 ? sz[1] : 0;
-    im.tiles0 = (int)fwd_pass_tiles(n, im.s0, kFwdWNarrow);
+    im.s0 = ip.s0;
+    im.s1 = ip.s1;
+    im.tiles0 = (int)ragged_items(ip.tiles0, ip.kind0, ip.s0);  // pass-0 items the counter reaches
+    im.kind0 = ip.kind0;
+    im.kind1 = ip.kind1;
+    im.cs = ip.cs;
+    im.pad = 0;
     // Fault injection for tests: the image's second pass waits for one more
     // first-pass tile than exists, so its wait can only expire.
     if (i == starve_image && im.s1 > 0) im.tiles0 += 1;
     in_off += n * n;
     out_off += 4 * n * (2 * n - 1);
-    if (P == 2) inter_off += 4 * n * (2 * n - 1);
+    inter_off += ragged_inter_slot(n, sizeof(T));
   }
   // Items: first passes (largest images first), then second passes.
   std::vector<i64> order((size_t)count);
@@ -558,11 +681,11 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
   items.reserve((size_t)p.n_items);
   for (int pass = 0; pass < 2; ++pass)
     for (i64 oi : order) {
-      const RaggedImage &im = imgs[(size_t)oi];
-      const int S = pass == 0 ? im.s0 : im.s1;
-      if (pass == 1 && im.s1 == 0) continue;
-      const i64 nt = fwd_pass_tiles(im.n, S, kFwdWNarrow);
-      for (i64 t = 0; t < nt; ++t) items.push_back(RaggedItem{(int)oi, pass, (int)t, 0});
+      const RaggedImagePlan &ip = plans[(size_t)oi];
+      const i64 nt = pass == 0 ? ip.tiles0 : ip.tiles1;
+      const int g = ragged_group(pass == 0 ? ip.kind0 : ip.kind1, pass == 0 ? ip.s0 : ip.s1);
+      for (i64 t = 0; t < nt; t += g)
+        items.push_back(RaggedItem{(int)oi, pass, (int)t, (int)(nt - t < g ? nt - t : g)});
     }
   char *base = static_cast<char *>(ws);
   if (cudaMemcpyAsync(base + p.off_imgs, imgs.data(), sizeof(RaggedImage) * imgs.size(),
@@ -572,7 +695,9 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
       cudaMemsetAsync(base + p.off_ctl, 0, sizeof(unsigned) * (size_t)(2 + count), st) != cudaSuccess)
     return ADRT_GB300_ERR_CUDA;
   // The copies above are from pageable memory: they complete before the calls return.
-  constexpr size_t smem = 2 * sizeof(T) * FwdTile<T, 32, kFwdWNarrow>::BUF;
+  // float32 items may be fast-pass tiles, which need fast::SMEM.
+  constexpr size_t smem_generic = 2 * sizeof(T) * FwdTile<T, 32, kFwdWNarrow>::BUF;
+  constexpr size_t smem = sizeof(T) == 4 && fast::SMEM > smem_generic ? fast::SMEM : smem_generic;
   auto kern = ragged_fwd_kernel<T>;
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)kern, smem, configured)) return rc;
@@ -582,13 +707,14 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFwdThreads, smem);
   if (per_sm < 1) per_sm = 1;
   i64 grid = (i64)sms * per_sm;
-  if (grid > p.n_items) grid = p.n_items;
+  const i64 n_items = (i64)items.size();  // <= p.n_items, the layout's capacity
+  if (grid > n_items) grid = n_items;
   if (grid < 1) return ADRT_GB300_OK;
   unsigned *ctl = reinterpret_cast<unsigned *>(base + p.off_ctl);
   kern<<<(unsigned)grid, kFwdThreads, smem, st>>>(
       in, out, reinterpret_cast<T *>(base + p.off_inter),
       reinterpret_cast<const RaggedImage *>(base + p.off_imgs),
-      reinterpret_cast<const RaggedItem *>(base + p.off_items), (int)p.n_items, ctl, ctl + 2,
+      reinterpret_cast<const RaggedItem *>(base + p.off_items), (int)n_items, ctl, ctl + 2,
       wait_ns ? wait_ns : kRaggedWaitNs);
   return launch_status();
 }

@@ -302,9 +302,12 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   // The pass kernels index one quadrant (n (2n-1) elements) in 32 bits.
   if (n > 32768) return ADRT_GB300_ERR_TOO_LARGE;
   int sizes[16];
-  const int P = plan_bwd(n, sizeof(T), sizes);
-  const bool fast = bwd_fast_eligible(n, sizeof(T));
-  const i64 cs = bwd_cs(n, sizeof(T));
+  int P = plan_bwd(n, sizeof(T), sizes);
+  // Unaligned buffers take the generic passes (unpadded rows fit in the
+  // workspace sized for padded ones).
+  const bool fast = bwd_fast_eligible(n, sizeof(T)) && aligned32(in) && aligned32(out);
+  const i64 cs = fast ? bwd_cs(n, sizeof(T)) : 2 * n - 1;
+  if (!fast && bwd_fast_eligible(n, sizeof(T))) P = plan_passes_bwd(n, sizeof(T), sizes);
   const size_t per = (size_t)4 * n * cs * sizeof(T);
   const int nbuf = P <= 1 ? 0 : (P >= 3 ? 2 : 1);
   i64 chunk = bwd_chunk(batch, n, sizeof(T));

@@ -65,6 +65,11 @@ inline size_t dtype_size(int dtype) {
 
 inline int ceil_div_i(i64 a, i64 b) { return (int)((a + b - 1) / b); }
 
+// The fast float32 kernels load and store 16- and 32-byte vectors: they run
+// only on buffers that are 32-byte aligned (every cudaMalloc or torch
+// allocation is); others take the generic kernels.
+inline bool aligned32(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
+
 // Count of kernel launches enqueued by this library (reported through
 // adrt_gb300_launch_count); defined in capi.cu.
 void count_launch();
