@@ -22,6 +22,8 @@
 // directly (the transpose is fused into its store).  Passes in between use a
 // workspace laid out like the reference's buffer: [b][q][R][A][2n-1].
 #include <algorithm>
+#include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -635,6 +637,23 @@ size_t ragged_workspace_bytes(const int64_t *sizes, i64 count, size_t elem, int 
   return *rc ? 0 : p.total;
 }
 
+// Pinned host staging for a launch's descriptors, one per device, so that
+// their upload is asynchronous (a copy from pageable memory would first wait
+// for the stream's earlier work).  Reused once its previous upload has
+// completed (an event recorded after it); grown as needed.  The first call
+// on a device allocates it: that call should come before any stream capture.
+struct RaggedStaging {
+  std::mutex mu;
+  void *host = nullptr;
+  size_t cap = 0;
+  cudaEvent_t done = nullptr;
+};
+
+static RaggedStaging &ragged_staging(int dev) {
+  static RaggedStaging st[64];
+  return st[dev & 63];
+}
+
 // Wall-clock bound on one wait (the whole batch runs in far less).
 constexpr unsigned long long kRaggedWaitNs = 4000000000ull;
 
@@ -688,13 +707,31 @@ int adrt_ragged(const T *in, T *out, const int64_t *sizes, i64 count, void *ws, 
         items.push_back(RaggedItem{(int)oi, pass, (int)t, (int)(nt - t < g ? nt - t : g)});
     }
   char *base = static_cast<char *>(ws);
-  if (cudaMemcpyAsync(base + p.off_imgs, imgs.data(), sizeof(RaggedImage) * imgs.size(),
-                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(base + p.off_items, items.data(), sizeof(RaggedItem) * items.size(),
-                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemsetAsync(base + p.off_ctl, 0, sizeof(unsigned) * (size_t)(2 + count), st) != cudaSuccess)
-    return ADRT_GB300_ERR_CUDA;
-  // The copies above are from pageable memory: they complete before the calls return.
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ADRT_GB300_ERR_CUDA;
+    RaggedStaging &sg = ragged_staging(dev);
+    std::lock_guard<std::mutex> lock(sg.mu);
+    const size_t bi = sizeof(RaggedImage) * imgs.size(), bt = sizeof(RaggedItem) * items.size();
+    if (sg.done == nullptr && cudaEventCreateWithFlags(&sg.done, cudaEventDisableTiming) != cudaSuccess)
+      return ADRT_GB300_ERR_CUDA;
+    if (cudaEventSynchronize(sg.done) != cudaSuccess) return ADRT_GB300_ERR_CUDA;  // previous upload done
+    if (sg.cap < bi + bt) {
+      if (sg.host) cudaFreeHost(sg.host);
+      sg.host = nullptr;
+      sg.cap = 0;
+      if (cudaMallocHost(&sg.host, bi + bt) != cudaSuccess) return ADRT_GB300_ERR_CUDA;
+      sg.cap = bi + bt;
+    }
+    char *h = static_cast<char *>(sg.host);
+    std::memcpy(h, imgs.data(), bi);
+    std::memcpy(h + bi, items.data(), bt);
+    if (cudaMemcpyAsync(base + p.off_imgs, h, bi, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(base + p.off_items, h + bi, bt, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaEventRecord(sg.done, st) != cudaSuccess ||
+        cudaMemsetAsync(base + p.off_ctl, 0, sizeof(unsigned) * (size_t)(2 + count), st) != cudaSuccess)
+      return ADRT_GB300_ERR_CUDA;
+  }
   // float32 items may be fast-pass tiles, which need fast::SMEM.
   constexpr size_t smem_generic = 2 * sizeof(T) * FwdTile<T, 32, kFwdWNarrow>::BUF;
   constexpr size_t smem = sizeof(T) == 4 && fast::SMEM > smem_generic ? fast::SMEM : smem_generic;

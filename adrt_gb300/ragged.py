@@ -20,7 +20,7 @@ from . import _lib
 from ._ops import iadrt as _iadrt
 from ._wrappers import float_code, is_pow2
 
-__all__ = ["adrt_ragged", "iadrt_ragged", "iadrt_fmg_ragged"]
+__all__ = ["adrt_ragged", "RaggedPlan", "iadrt_ragged", "iadrt_fmg_ragged"]
 
 
 def _sizes_array(images):
@@ -43,25 +43,9 @@ def _sizes_array(images):
 
 def _launch(images, wait_ns=0, starve_image=-1):
     sizes, dt, dev = _sizes_array(images)
-    code = float_code(images[0])
-    lib = _lib.load()
-    sp = sizes.ctypes.data_as(ctypes.c_void_p)
-    nbytes = ctypes.c_size_t(0)
-    _lib.check(lib.adrt_gb300_ragged_workspace_size(sp, len(sizes), code, ctypes.byref(nbytes)), "ragged")
-    ws = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=dev)
-    packed = torch.cat([im.contiguous().reshape(-1) for im in images])
-    outn = [4 * n * (2 * n - 1) for n in sizes]
-    out = torch.empty(sum(outn), dtype=dt, device=dev)
-    stream = torch.cuda.current_stream(dev).cuda_stream
-    rc = lib.adrt_gb300_adrt_ragged_ex(packed.data_ptr(), out.data_ptr(), sp, len(sizes), code,
-                                       ws.data_ptr(), nbytes.value, wait_ns, starve_image, stream)
-    _lib.check(rc, "adrt_ragged")
-    status = lib.adrt_gb300_ragged_status(ws.data_ptr(), sp, len(sizes), code, stream)
-    views, off = [], 0
-    for n, k in zip(sizes, outn):
-        views.append(out[off:off + k].view(4, 2 * int(n) - 1, int(n)))
-        off += k
-    return views, status
+    plan = RaggedPlan(sizes, dt, dev)
+    plan.launch(plan.packed_input(images), wait_ns, starve_image)
+    return plan.views(), plan.status()
 
 
 def adrt_ragged(images):
@@ -71,6 +55,60 @@ def adrt_ragged(images):
     views, status = _launch(images)
     _lib.check(status, "adrt_ragged")
     return views
+
+
+class RaggedPlan:
+    """Buffers for repeated ragged launches over one list of sizes: the
+    workspace and the packed output, allocated once.  `packed_input(images)`
+    packs a list of images into one buffer (image after image, row-major);
+    `launch(packed)` runs the persistent launch on torch's current stream and
+    returns without waiting; `status()` then reads the launch's error word
+    (waiting for the launch) and `views()` gives the (4, 2n-1, n) results."""
+
+    def __init__(self, sizes, dtype=torch.float32, device="cuda"):
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        if self.sizes.ndim != 1 or self.sizes.size == 0:
+            raise ValueError("sizes must be a non-empty list of image sides")
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.code = float_code(torch.empty(0, dtype=dtype))
+        lib = _lib.load()
+        self._sp = self.sizes.ctypes.data_as(ctypes.c_void_p)
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(lib.adrt_gb300_ragged_workspace_size(self._sp, len(self.sizes), self.code,
+                                                        ctypes.byref(nbytes)), "ragged")
+        self.ws = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=self.device)
+        self.ws_bytes = nbytes.value
+        self.in_elems = int((self.sizes * self.sizes).sum())
+        self.out_lengths = [4 * int(n) * (2 * int(n) - 1) for n in self.sizes]
+        self.out = torch.empty(sum(self.out_lengths), dtype=dtype, device=self.device)
+
+    def packed_input(self, images):
+        return torch.cat([im.contiguous().reshape(-1) for im in images])
+
+    def launch(self, packed, wait_ns=0, starve_image=-1):
+        if not (isinstance(packed, torch.Tensor) and packed.device == self.out.device
+                and packed.dtype == self.dtype and packed.is_contiguous()
+                and packed.numel() == self.in_elems):
+            raise ValueError("packed input must be one contiguous %s buffer of %d elements on %s"
+                             % (self.dtype, self.in_elems, self.out.device))
+        stream = torch.cuda.current_stream(self.out.device).cuda_stream
+        rc = _lib.load().adrt_gb300_adrt_ragged_ex(packed.data_ptr(), self.out.data_ptr(), self._sp,
+                                                   len(self.sizes), self.code, self.ws.data_ptr(),
+                                                   self.ws_bytes, wait_ns, starve_image, stream)
+        _lib.check(rc, "adrt_ragged")
+
+    def status(self):
+        stream = torch.cuda.current_stream(self.out.device).cuda_stream
+        return _lib.load().adrt_gb300_ragged_status(self.ws.data_ptr(), self._sp, len(self.sizes),
+                                                    self.code, stream)
+
+    def views(self):
+        views, off = [], 0
+        for n, k in zip(self.sizes, self.out_lengths):
+            views.append(self.out[off:off + k].view(4, 2 * int(n) - 1, int(n)))
+            off += k
+        return views
 
 
 def iadrt_ragged(arrays):

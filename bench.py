@@ -435,7 +435,7 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
 
     import adrt_gb300 as adrt
     from adrt_gb300.data import ragged_phantoms
-    from adrt_gb300.ragged import adrt_ragged, iadrt_fmg_ragged, iadrt_ragged
+    from adrt_gb300.ragged import RaggedPlan, adrt_ragged, iadrt_fmg_ragged, iadrt_ragged
 
     imgs = ragged_phantoms(count, seed=0, device=dev)
 
@@ -454,6 +454,22 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
             gc.enable()
 
     ys, t_fwd = timed(lambda: adrt_ragged(imgs), 3)
+    # The persistent launch alone, on an input already packed into one buffer
+    # (the list API above also packs, plans and allocates on every call).
+    plan = RaggedPlan([int(m.shape[-1]) for m in imgs], torch.float32, dev)
+    packed = plan.packed_input(imgs)
+    for _ in range(3):
+        plan.launch(packed)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    ev0.record()
+    for _ in range(reps):
+        plan.launch(packed)
+    ev1.record()
+    torch.cuda.synchronize()
+    t_dev = ev0.elapsed_time(ev1) / 1e3 / reps
+    plan_ok = plan.status() == 0 and all(torch.equal(a, b) for a, b in zip(plan.views(), ys))
     inv, t_inv = timed(lambda: iadrt_ragged(ys), 3)
     sub = list(range(fmg_sample))
     fmg, t_fmg = timed(lambda: iadrt_fmg_ragged([ys[i] for i in sub]), 1)
@@ -477,6 +493,11 @@ def ragged_bench(torch, dev, count=1024, fmg_sample=1024):
         "counts": {str(n): sum(1 for m in imgs if m.shape[-1] == n) for n in sizes},
         "adrt_img_s": count / t_fwd,
         "adrt_ms": 1e3 * t_fwd,
+        "adrt_packed_img_s": count / t_dev,
+        "adrt_packed_ms": 1e3 * t_dev,
+        "adrt_packed_note": ("one persistent launch per step on a pre-packed input, "
+                             "10 back-to-back launches timed with CUDA events; results equal the list API's: "
+                             + str(plan_ok)),
         "iadrt_img_s": count / t_inv,
         "iadrt_fmg_img_s": fmg_sample / t_fmg,
         "iadrt_fmg_sample": fmg_sample,

@@ -67,3 +67,29 @@ def test_ragged_rejects():
         ragged.adrt_ragged([torch.zeros((2048, 2048), device="cuda")])
     with pytest.raises(ValueError, match="power of two"):
         ragged.adrt_ragged([torch.zeros((6, 6), device="cuda")])
+
+
+def test_ragged_plan_repeated_launches():
+    # One plan, several back-to-back launches on one stream (descriptor
+    # uploads staged through pinned memory), then a second plan whose
+    # descriptors are larger: results equal the list API's bit for bit.
+    sizes = [1024, 32, 256, 64, 1024, 128, 512]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    imgs = [torch.randn((n, n), generator=g, device="cuda") for n in sizes]
+    want = ragged.adrt_ragged(imgs)
+    plan = ragged.RaggedPlan(sizes)
+    packed = plan.packed_input(imgs)
+    for _ in range(4):
+        plan.launch(packed)
+    assert plan.status() == 0
+    for a, b in zip(plan.views(), want):
+        assert bits_equal(a.cpu().numpy(), b.cpu().numpy())
+    big = ragged.RaggedPlan(sizes * 40)
+    big.launch(big.packed_input(imgs * 40))
+    plan.launch(packed)
+    assert big.status() == 0 and plan.status() == 0
+    for a, b in zip(big.views(), want * 40):
+        assert bits_equal(a.cpu().numpy(), b.cpu().numpy())
+    with pytest.raises(ValueError, match="packed input"):
+        plan.launch(packed[:-1])
