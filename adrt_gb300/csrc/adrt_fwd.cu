@@ -437,7 +437,7 @@ __device__ __noinline__ void ragged_generic_item(int S, const FwdPassArgs a, i64
 }
 
 __device__ __forceinline__ void ragged_fast_a_item(const float *img, float *inter_img, int t, float *xs) {
-  fast::pass_a_tile<true>(img, inter_img, t / (fast::A_TILES * 32), (t / fast::A_TILES) % 32, t % fast::A_TILES,
+  fast::pass_a_tile<5, true>(img, inter_img, t / (fast::A_TILES * 32), (t / fast::A_TILES) % 32, t % fast::A_TILES,
                          xs);
 }
 

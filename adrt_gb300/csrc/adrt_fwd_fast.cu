@@ -9,17 +9,30 @@
 namespace adrtg {
 namespace fast {
 
-// inter layout: [image][q][row group g (32)][angle a (32)][CS]
+// The first S stages for n = 32 * 2^S.  inter layout: [image][q][row group g
+// (32)][angle a (2^S)][CS]; grid (column tile, 32-row block R, quadrant,
+// image), column tile fastest.
+template <int S>
 __global__ void __launch_bounds__(NT, 2) pass_a_kernel(const float *__restrict__ in,
-                                                       float *__restrict__ inter, int nimg) {
+                                                       float *__restrict__ inter) {
+  using P = PassA<S>;
   extern __shared__ __align__(16) float xs[];
-  int t = blockIdx.x;
-  const int ct = t % A_TILES; t /= A_TILES;
-  const int r = t % 32; t /= 32;
-  const int q = t % 4; t /= 4;
-  const int bimg = t;
-  (void)nimg;
-  pass_a_tile(in + (size_t)bimg * N * N, inter + (size_t)bimg * 4 * 32 * 32 * CS, q, r, ct, xs);
+  unsigned t = blockIdx.x;
+  const int ct = (int)(t % (unsigned)P::TILES); t /= (unsigned)P::TILES;
+  const int R = (int)(t % (unsigned)(P::n / 32)); t /= (unsigned)(P::n / 32);
+  const int q = (int)(t & 3u);
+  const size_t bimg = t >> 2;
+  pass_a_tile<S>(in + bimg * P::n * P::n, inter + bimg * 4 * P::n * P::CS, q, R, ct, xs);
+}
+
+template <int S>
+static int launch_pass_a(const float *in, float *inter, int nb, cudaStream_t st) {
+  using P = PassA<S>;
+  static std::atomic<unsigned long long> configured{0};
+  if (const int rc = smem_limit_once((const void *)pass_a_kernel<S>, SMEM, configured)) return rc;
+  const unsigned grid = (unsigned)nb * 4u * (unsigned)(P::n / 32) * (unsigned)P::TILES;
+  pass_a_kernel<S><<<grid, NT, SMEM, st>>>(in, inter);
+  return launch_status();
 }
 
 // Pass B for any n >= 64: the last five stages.  inter layout per image:
@@ -52,6 +65,9 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
 // aligned); pass B reads anything past the row end as +0.  n = 1024: 1056.
 static int fast_cs(i64 n) { return (int)((n + n / 32 - 1 + 7) / 8 * 8); }
 static_assert(fast::CS == (fast::N + fast::N / 32 - 1 + 7) / 8 * 8, "row stride at n = 1024");
+static_assert(fast::PassA<5>::CS == fast::CS && fast::PassA<4>::CS == 528 && fast::PassA<3>::CS == 264 &&
+                  fast::PassA<2>::CS == 136,
+              "pass A row strides equal the intermediate's");
 
 int fast_inter_cs(i64 n) { return fast_cs(n); }
 
@@ -108,8 +124,7 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
   if (ws == nullptr || (i64)ws_bytes < per) return ADRT_GB300_ERR_WORKSPACE;
   unsigned *err = fast_error_word();
   if (!err) return ADRT_GB300_ERR_CUDA;
-  static std::atomic<unsigned long long> configured_a{0}, configured_b{0};
-  if (const int rc = smem_limit_once((const void *)fast::pass_a_kernel, fast::SMEM, configured_a)) return rc;
+  static std::atomic<unsigned long long> configured_b{0};
   if (const int rc = smem_limit_once((const void *)fast::pass_b_kernel, fast::SMEM, configured_b)) return rc;
   i64 chunk = fast_chunk(batch, n);
   if ((i64)ws_bytes < per * chunk) chunk = (i64)ws_bytes / per;
@@ -120,12 +135,18 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
   for (i64 b0 = 0; b0 < batch; b0 += chunk) {
     const int nb = (int)((batch - b0) < chunk ? (batch - b0) : chunk);
     int rc;
-    if (n == fast::N) {
-      const unsigned grid = (unsigned)(nb * 4 * 32 * fast::A_TILES);
-      fast::pass_a_kernel<<<grid, fast::NT, fast::SMEM, st>>>(in + b0 * n * n, inter, nb);
-      rc = launch_status();
+    // First L-5 stages: the register pass for n >= 128, the generic pass at
+    // n = 64 (one stage).
+    const float *src = in + b0 * n * n;
+    if (n >= 128) {
+      switch (L) {
+        case 10: rc = fast::launch_pass_a<5>(src, inter, nb, st); break;
+        case 9: rc = fast::launch_pass_a<4>(src, inter, nb, st); break;
+        case 8: rc = fast::launch_pass_a<3>(src, inter, nb, st); break;
+        default: rc = fast::launch_pass_a<2>(src, inter, nb, st); break;
+      }
     } else {
-      rc = fwd_first_pass_padded(in + b0 * n * n, inter, nb, n, L - 5, cs, st);
+      rc = fwd_first_pass_padded(src, inter, nb, n, L - 5, cs, st);
     }
     if (rc) return rc;
     const dim3 gridb((unsigned)(col_tiles * 4), (unsigned)nb, (unsigned)(n / 32));

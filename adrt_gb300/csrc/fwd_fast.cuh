@@ -45,7 +45,22 @@ constexpr int N = 1024;
 // that reach a stored offset run.
 constexpr int A_TILES = (N + 31 + W - 1) / W;  // 3
 constexpr int CS = (N + 31 + 7) / 8 * 8;       // 1056: intermediate row stride (128-byte multiple)
+static_assert(A_TILES == 3 && CS == 1056, "n = 1024 pass A geometry");
 constexpr unsigned FULL = 0xffffffffu;
+
+// Pass A for n = 32 * 2^S (S = 2..5): the first S stages, after which the
+// image's 32 row groups of 2^S rows each have 2^S angles.  A CTA still owns
+// 32 consecutive image rows (or columns), i.e. 32 >> S row groups (one at
+// S = 5, eight at S = 2), and the intermediate keeps each row's support:
+// offsets below n + 2^S - 1, rounded up to 8 floats.
+template <int S>
+struct PassA {
+  static_assert(S >= 2 && S <= 5, "pass A runs 2 to 5 stages");
+  static constexpr int n = 32 << S;
+  static constexpr int CS = (n + n / 32 - 1 + 7) / 8 * 8;  // 1056, 528, 264, 136
+  static constexpr int TILES = (CS + W - 1) / W;            // 3, 2, 1, 1
+  static constexpr int GS = S - 2;                          // stages of group 2
+};
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange buffer");
 
@@ -188,7 +203,7 @@ __device__ __forceinline__ float4 ld4_fill(const float *p, int g0, int lim) {
 
 // Pass A, quadrants 0 and 3: members are image rows, positions run along the
 // row from its right end (offset c <-> column n-1-c).  Warp = member quad.
-template <int NIT = 0>
+template <int NI, int NIT = 0>
 __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r, int tbase, int pos,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, mq = threadIdx.x >> 5;
@@ -202,8 +217,8 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
       const int R0 = 32 * r + 4 * mq + jj;
-      const int irow = (q == 0) ? R0 : (N - 1 - R0);
-      raw[it][jj] = ld4_fill<LD_CA>(img + irow * N + (N - 4 - ref0), ref0, N);
+      const int irow = (q == 0) ? R0 : (NI - 1 - R0);
+      raw[it][jj] = ld4_fill<LD_CA>(img + irow * NI + (NI - 4 - ref0), ref0, NI);
     }
   }
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
@@ -228,6 +243,7 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
 // position group = lane >> 3; warp w sweeps chunks [16w - 1, 16w + 16), the
 // first one only to seed the boundary values.  Warps whose chunks start at or
 // beyond `pos` have nothing to produce.
+template <int NI>
 __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r, int tbase, int pos,
                                                   float *xs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -243,9 +259,9 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int ref = ref0 + k;
-      const int irow = (q == 2) ? ref : (N - 1 - ref);
+      const int irow = (q == 2) ? ref : (NI - 1 - ref);
       // A chunk past this warp's range only seeds nothing: load it as absent.
-      raw[it][k] = ld4_fill<LD_CA>(img + irow * N + 32 * r + 4 * mq, live ? ref : -1, N);
+      raw[it][k] = ld4_fill<LD_CA>(img + irow * NI + 32 * r + 4 * mq, live ? ref : -1, NI);
     }
   }
   G1Tail saved{-0.f, -0.f, -0.f, -0.f, -0.f};
@@ -328,16 +344,20 @@ __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase
 // ---------------------------------------------------------------------------
 // Group 2: stages 2-4 for angle L1 of group 1; lane owns 8 combos x 8
 // positions (block b).  Returns out[l][k], l = local angle (tile angle 8*L1 + l).
+// GS < 3 (pass A with S = GS + 2 stages): the 8 combos form 8 >> GS
+// independent sets of 2^GS (one per row group), each merged by GS stages:
+// combo h is pre-shifted by L1 * (h mod 2^GS), and out[e] holds set
+// e >> GS at local angle e mod 2^GS (row-group angle 2^GS * L1 + that).
 // ---------------------------------------------------------------------------
-template <int L1, int XL = 0>
+template <int L1, int XL = 0, int GS = 3>
 __device__ __forceinline__ void group2_compute(const float *xs, int b, bool active,
                                                float (&out)[8][8]) {
+  static_assert(GS >= 0 && GS <= 3, "group 2 runs 0 to 3 stages");
   float r[8][8];
 #pragma unroll
   for (int h = 0; h < 8; ++h) {
-    constexpr int dummy = 0;
-    (void)dummy;
-    const int qh = (L1 * h) >> 2, mh = (L1 * h) & 3;
+    const int hl = h & ((1 << GS) - 1);
+    const int qh = (L1 * hl) >> 2, mh = (L1 * hl) & 3;
     float4 B = make_float4(0.f, 0.f, 0.f, 0.f), Cc = B, A = B;
     const float *row = xs + xrow<XL>(h, L1) * RS;
     if (active) {
@@ -362,6 +382,13 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
       }
     }
   }
+  if constexpr (GS == 0) {
+#pragma unroll
+    for (int h = 0; h < 8; ++h)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[h][k] = r[h][k];
+    return;
+  }
   // stage a: pairs (2P, 2P+1), shift p.
   float t0[4][2][8];
 #pragma unroll
@@ -372,6 +399,13 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
       add_rn2(r[2 * P][k], r[2 * P][k + 1], r[2 * P + 1][k], r[2 * P + 1][k + 1], t0[P][0][k], t0[P][0][k + 1]);
 #pragma unroll
     for (int k = 0; k < 8; ++k) t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
+  }
+  if constexpr (GS == 1) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[e][k] = t0[e >> 1][e & 1][k];
+    return;
   }
   // stage b: combos (2Q, 2Q+1), li in {0,1}, shift li + p.
   float t1[2][4][8];
@@ -398,6 +432,13 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
         }
       }
     }
+  }
+  if constexpr (GS == 2) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[e][k] = t1[e >> 2][e & 3][k];
+    return;
   }
   // stage c: li in [0,4), shift li + p.
 #pragma unroll
@@ -436,18 +477,26 @@ __device__ __forceinline__ void group2_lane(int &b, bool &active, bool &store) {
 // block 31.
 __device__ __forceinline__ int first_stored_block() { return (threadIdx.x >> 7) ? 31 : 0; }
 
-template <int L1>
-__device__ __forceinline__ void group2_passA(const float *xs, float *dst_rows, int c0) {
-  if (c0 + 8 * first_stored_block() >= CS) return;  // nothing this half stores
+// Pass A's group 2 for S stages: stores the 8 rows of this lane's block.
+// Row e of `out` is row group (32 >> S) R + (e >> GS) at angle 2^GS L1 +
+// (e mod 2^GS); inter_q = the quadrant's intermediate [g (32)][a (2^S)][CS].
+template <int L1, int S>
+__device__ __forceinline__ void group2_passA(const float *xs, float *inter_q, int R, int c0) {
+  using P = PassA<S>;
+  if (c0 + 8 * first_stored_block() >= P::CS) return;  // nothing this half stores
   int b;
   bool active, store;
   group2_lane(b, active, store);
   float out[8][8];
-  group2_compute<L1>(xs, b, active, out);
+  group2_compute<L1, 0, P::GS>(xs, b, active, out);
   const int d0 = c0 + 8 * b;
-  if (store && d0 < CS) {
+  if (store && d0 < P::CS) {
 #pragma unroll
-    for (int l = 0; l < 8; ++l) st8(dst_rows + (size_t)(8 * L1 + l) * CS + d0, out[l]);
+    for (int e = 0; e < 8; ++e) {
+      const int g = (R << (3 - P::GS)) + (e >> P::GS);
+      const int a = (L1 << P::GS) + (e & ((1 << P::GS) - 1));
+      st8(inter_q + ((size_t)g * (1 << S) + a) * P::CS + d0, out[e]);
+    }
   }
 }
 
@@ -520,28 +569,29 @@ __device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q,
 }
 
 
-// One pass-A tile (n = 1024): quadrant q, row group r, column tile ct of one
-// image; inter_img = that image's intermediate [q][g (32)][a (32)][CS].
-// FULL_SWEEP: every tile sweeps all positions (a persistent loop around a
-// sweep of run-time length spills; the positions past the stored ones are
-// computed and dropped).
-template <bool FULL_SWEEP = false>
-__device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, int q, int r, int ct, float *xs) {
+// One pass-A tile (n = 32 * 2^S): quadrant q, rows (or columns) 32 R ..
+// 32 R + 31, column tile ct of one image; inter_img = that image's
+// intermediate [q][g (32)][a (2^S)][CS].  FULL_SWEEP: every tile sweeps all
+// positions (a persistent loop around a sweep of run-time length spills; the
+// positions past the stored ones are computed and dropped).
+template <int S, bool FULL_SWEEP = false>
+__device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, int q, int R, int ct, float *xs) {
+  using P = PassA<S>;
   const int c0 = ct * W, tbase = c0 - HALO;
-  const int pos = needed_positions(min(W, CS - c0));
+  const int pos = needed_positions(min(W, P::CS - c0));
   if (q == 0 || q == 3) {
-    if (FULL_SWEEP || pos == TW) group1_passA_rows<NCH / 32>(img, q, r, tbase, pos, xs);
-    else group1_passA_rows(img, q, r, tbase, pos, xs);
+    if (FULL_SWEEP || pos == TW) group1_passA_rows<P::n, NCH / 32>(img, q, R, tbase, pos, xs);
+    else group1_passA_rows<P::n>(img, q, R, tbase, pos, xs);
   } else {
-    group1_passA_cols(img, q, r, tbase, pos, xs);
+    group1_passA_cols<P::n>(img, q, R, tbase, pos, xs);
   }
   __syncthreads();
-  float *dst_rows = inter_img + ((size_t)q * 32 + r) * 32 * CS;
+  float *inter_q = inter_img + (size_t)q * P::n * P::CS;
   switch ((threadIdx.x >> 5) & 3) {
-    case 0: group2_passA<0>(xs, dst_rows, c0); break;
-    case 1: group2_passA<1>(xs, dst_rows, c0); break;
-    case 2: group2_passA<2>(xs, dst_rows, c0); break;
-    default: group2_passA<3>(xs, dst_rows, c0); break;
+    case 0: group2_passA<0, S>(xs, inter_q, R, c0); break;
+    case 1: group2_passA<1, S>(xs, inter_q, R, c0); break;
+    case 2: group2_passA<2, S>(xs, inter_q, R, c0); break;
+    default: group2_passA<3, S>(xs, inter_q, R, c0); break;
   }
 }
 

@@ -169,6 +169,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
+def link_bandwidth(torch, dev, nbytes=1 << 30, reps=4):
+    """Host<->device bandwidth of this GPU's link: pinned 1 GiB copies each
+    way (copy engine, CUDA events), GB/s.  SM-driven copies into pinned host
+    memory and several copy streams measured the same on GB300 (193 GB/s
+    device-to-host, 211 GB/s host-to-device): the link, not the copy method,
+    is the limit."""
+    d = torch.empty(nbytes // 4, device=dev)
+    h = torch.empty(nbytes // 4, pin_memory=True)
+    out = {}
+    for name, fn in (("d2h_gbs", lambda: h.copy_(d, non_blocking=True)),
+                     ("h2d_gbs", lambda: d.copy_(h, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = nbytes * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del d, h
+    return out
+
+
 def _host_mem_gb():
     """(total, available) host memory in GB from /proc/meminfo, or None."""
     try:
@@ -747,6 +771,13 @@ def main():
             windows.append(max_over_ranks(time.perf_counter() - t0))
             gc.enable()
         t_e2e = min(windows)
+        # The link roofline: the two directions overlap (separate copy
+        # streams), so a step takes at least its larger copy's time.
+        link = link_bandwidth(torch, dev)
+        bi, bo = xh.numel() * xh.element_size(), yh.numel() * yh.element_size()
+        link_s = max(bi / (link["h2d_gbs"] * 1e9), bo / (link["d2h_gbs"] * 1e9))
+        link["bound"] = world * B / link_s
+        link["frac"] = (world * B * args.e2e_steps / t_e2e) / link["bound"]
         e2e = {
             "value": world * B * args.e2e_steps / t_e2e,
             "unit": UNIT,
@@ -757,6 +788,7 @@ def main():
             "warmup_call_ms": warm_ms,
             "call_ms": call_ms,
             "host_mem_gb": _host_mem_gb(),
+            "link": link,
         }
         del yh
 
