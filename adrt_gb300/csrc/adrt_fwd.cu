@@ -436,9 +436,22 @@ __device__ __noinline__ void ragged_generic_item(int S, const FwdPassArgs a, i64
   ragged_tile_S<T, FIRST, LAST>(S, a, tile, smem);
 }
 
-__device__ __forceinline__ void ragged_fast_a_item(const float *img, float *inter_img, int t, float *xs) {
-  fast::pass_a_tile<5, true>(img, inter_img, t / (fast::A_TILES * 32), (t / fast::A_TILES) % 32, t % fast::A_TILES,
-                         xs);
+// Register first pass of n = 32 * 2^S: item t = (quadrant, 32-row block R,
+// column tile), column tile fastest.
+template <int S>
+__device__ __forceinline__ void ragged_fast_a_tile(const float *img, float *inter_img, int t, float *xs) {
+  using P = fast::PassA<S>;
+  fast::pass_a_tile<S, true>(img, inter_img, t / (P::TILES * (P::n / 32)), (t / P::TILES) % (P::n / 32),
+                             t % P::TILES, xs);
+}
+
+__device__ __forceinline__ void ragged_fast_a_item(int S, const float *img, float *inter_img, int t, float *xs) {
+  switch (S) {
+    case 5: ragged_fast_a_tile<5>(img, inter_img, t, xs); break;
+    case 4: ragged_fast_a_tile<4>(img, inter_img, t, xs); break;
+    case 3: ragged_fast_a_tile<3>(img, inter_img, t, xs); break;
+    default: ragged_fast_a_tile<2>(img, inter_img, t, xs); break;
+  }
 }
 
 __device__ __forceinline__ void ragged_fast_b_item(const float *inter_img, float *out_img, int n, int cs, int t,
@@ -489,7 +502,7 @@ ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__
       float *xs = reinterpret_cast<float *>(smem_raw);
       const int kind = item.pass == 0 ? im.kind0 : im.kind1;
       if (kind == RAGGED_FAST_A)
-        ragged_fast_a_item(reinterpret_cast<const float *>(in) + im.in_off,
+        ragged_fast_a_item(im.s0, reinterpret_cast<const float *>(in) + im.in_off,
                            reinterpret_cast<float *>(inter) + im.inter_off, item.tile, xs);
       else if (kind == RAGGED_FAST_B)
         ragged_fast_b_item(reinterpret_cast<const float *>(inter) + im.inter_off,
@@ -576,9 +589,11 @@ static RaggedImagePlan ragged_image_plan(i64 n, size_t elem, bool fast) {
     ip.s0 = L - 5;
     ip.s1 = 5;
     ip.cs = fast_inter_cs(n);
-    ip.kind0 = n == fast::N ? RAGGED_FAST_A : RAGGED_GENERIC;
+    // n >= 128: the register first pass (S = L - 5 >= 2 stages); n = 64:
+    // the generic one.
+    ip.kind0 = n >= 128 ? RAGGED_FAST_A : RAGGED_GENERIC;
     ip.kind1 = RAGGED_FAST_B;
-    ip.tiles0 = n == fast::N ? 4 * 32 * fast::A_TILES : fwd_pass_tiles(n, ip.s0, kFwdWNarrow);
+    ip.tiles0 = n >= 128 ? 4 * (n / 32) * ((ip.cs + fast::W - 1) / fast::W) : fwd_pass_tiles(n, ip.s0, kFwdWNarrow);
     ip.tiles1 = 4 * (n / 32) * fast::pass_b_col_tiles((int)n);
     ip.inter_elems = 4 * n * ip.cs;
     return ip;
