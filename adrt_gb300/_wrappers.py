@@ -122,6 +122,23 @@ def is_host(a) -> bool:
     return isinstance(a, np.ndarray) or (isinstance(a, torch.Tensor) and not a.is_cuda)
 
 
+_PIPELINE_STREAMS = {}
+
+
+def _pipeline_streams(dev):
+    """The three copy/transform streams of `host_pipeline` on device `dev`,
+    created once: the device buffers of every call are then allocated on the
+    same stream and come back from the caching allocator's pool for that
+    stream (fresh pool streams per call left them on a different stream each
+    time)."""
+    import torch
+
+    key = dev.index
+    if key not in _PIPELINE_STREAMS:
+        _PIPELINE_STREAMS[key] = tuple(torch.cuda.Stream(device=dev) for _ in range(3))
+    return _PIPELINE_STREAMS[key]
+
+
 def host_pipeline(a, out_tail, chunk, run_chunk):
     """Transform a host array batch by batch with copies overlapped.
 
@@ -146,7 +163,7 @@ def host_pipeline(a, out_tail, chunk, run_chunk):
     # page faults on first touch (measured 119 vs ~5000 images/s end to end).
     hout = torch.empty((B, *out_tail), dtype=hin.dtype, pin_memory=True)
     cur = torch.cuda.current_stream(dev)
-    s_in, s_run, s_out = (torch.cuda.Stream(device=dev) for _ in range(3))
+    s_in, s_run, s_out = _pipeline_streams(dev)
     for s in (s_in, s_run, s_out):
         s.wait_stream(cur)
     k0 = min(chunk, B)

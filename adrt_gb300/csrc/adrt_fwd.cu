@@ -438,61 +438,114 @@ __device__ __noinline__ void ragged_generic_item(int S, const FwdPassArgs a, i64
 
 // Register first pass of n = 32 * 2^S: item t = (quadrant, 32-row block R,
 // column tile), column tile fastest.
-template <int S>
-__device__ __forceinline__ void ragged_fast_a_tile(const float *img, float *inter_img, int t, float *xs) {
+template <int S, class Hook>
+__device__ __forceinline__ void ragged_fast_a_tile(const float *img, float *inter_img, int t, float *xs,
+                                                   const Hook &hook) {
   using P = fast::PassA<S>;
   fast::pass_a_tile<S, true>(img, inter_img, t / (P::TILES * (P::n / 32)), (t / P::TILES) % (P::n / 32),
-                             t % P::TILES, xs);
+                             t % P::TILES, xs, hook);
 }
 
-__device__ __forceinline__ void ragged_fast_a_item(int S, const float *img, float *inter_img, int t, float *xs) {
+template <class Hook>
+__device__ __forceinline__ void ragged_fast_a_item(int S, const float *img, float *inter_img, int t, float *xs,
+                                                   const Hook &hook) {
   switch (S) {
-    case 5: ragged_fast_a_tile<5>(img, inter_img, t, xs); break;
-    case 4: ragged_fast_a_tile<4>(img, inter_img, t, xs); break;
-    case 3: ragged_fast_a_tile<3>(img, inter_img, t, xs); break;
-    default: ragged_fast_a_tile<2>(img, inter_img, t, xs); break;
+    case 5: ragged_fast_a_tile<5>(img, inter_img, t, xs, hook); break;
+    case 4: ragged_fast_a_tile<4>(img, inter_img, t, xs, hook); break;
+    case 3: ragged_fast_a_tile<3>(img, inter_img, t, xs, hook); break;
+    default: ragged_fast_a_tile<2>(img, inter_img, t, xs, hook); break;
   }
 }
 
+template <class Hook>
 __device__ __forceinline__ void ragged_fast_b_item(const float *inter_img, float *out_img, int n, int cs, int t,
-                                                float *xs) {
+                                                   float *xs, const Hook &hook) {
   const int ctn = fast::pass_b_col_tiles(n);
-  fast::pass_b_tile<fast::LD_CG, true>(inter_img, out_img, n, cs, (t / ctn) % 4, t / (ctn * 4), t % ctn, xs);
+  fast::pass_b_tile<fast::LD_CG, true>(inter_img, out_img, n, cs, (t / ctn) % 4, t / (ctn * 4), t % ctn, xs,
+                                       hook);
 }
+
+// Descriptors of the item a CTA works on and of the one it fetched next
+// (image -1: no item).
+struct RaggedSlots {
+  RaggedItem item[2];
+  RaggedImage image[2];
+};
+
+// Thread 0 only: item `t` (a ticket) and its image into slot `s`.
+__device__ __forceinline__ void ragged_fetch(RaggedSlots &sl, int s, unsigned t, int n_items,
+                                             const RaggedImage *__restrict__ imgs,
+                                             const RaggedItem *__restrict__ items) {
+  RaggedItem it;
+  it.image = -1;
+  if (t < (unsigned)n_items) {
+    it = items[t];
+    sl.image[s] = imgs[it.image];
+  }
+  sl.item[s] = it;
+}
+
+// Fetches the next item when a fast tile calls it (thread 0; the others do
+// nothing).
+struct RaggedPrefetch {
+  RaggedSlots *sl;
+  int s;
+  unsigned t;
+  int n_items;
+  const RaggedImage *imgs;
+  const RaggedItem *items;
+  __device__ __forceinline__ void operator()() const {
+    if (threadIdx.x == 0) ragged_fetch(*sl, s, t, n_items, imgs, items);
+  }
+};
 
 // ctl[0]: next ticket, ctl[1]: error word.
 // Two CTAs per SM: the persistent loop inlines every stage count, and without
 // a bound the compiler spends registers that halve the resident CTAs.
+// Each CTA claims its next ticket when it starts an item and reads that
+// item's descriptors during the current one (in a fast tile once its loads
+// are in flight, after a generic item's tiles), so that no item starts with
+// a chain of dependent global loads.  A CTA that has seen an image's first
+// pass complete does not poll that image's counter again.
 template <typename T>
 __global__ void __launch_bounds__(kFwdThreads, 2)
 ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__ inter,
                   const RaggedImage *__restrict__ imgs, const RaggedItem *__restrict__ items,
                   int n_items, unsigned *ctl, unsigned *counters, unsigned long long wait_ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int s_item;
+  __shared__ RaggedSlots sl;
   __shared__ int s_ok;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = (int)atomicAdd(&ctl[0], 1u);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= n_items) break;
-    const RaggedItem item = items[it];
-    const RaggedImage im = imgs[item.image];
+  __shared__ int s_seen;  // last image whose first pass this CTA saw complete
+  if (threadIdx.x == 0) {
+    ragged_fetch(sl, 0, atomicAdd(&ctl[0], 1u), n_items, imgs, items);
+    s_seen = -1;
+  }
+  __syncthreads();
+  for (int slot = 0;; slot ^= 1) {
+    const RaggedItem item = sl.item[slot];
+    if (item.image < 0) break;
+    const RaggedImage im = sl.image[slot];
+    unsigned next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(&ctl[0], 1u);
+    const RaggedPrefetch prefetch{&sl, slot ^ 1, next, n_items, imgs, items};
     if (item.pass == 1) {
       if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned long long t0 = global_ns();
-        const volatile unsigned *done = counters + item.image;
-        const volatile unsigned *err = ctl + 1;
-        while (*done < (unsigned)im.tiles0) {
-          if (*err != 0u || global_ns() - t0 > wait_ns) {
-            ok = 0;
-            atomicExch(&ctl[1], 1u);
-            break;
+        if (s_seen != item.image) {
+          const unsigned long long t0 = global_ns();
+          const volatile unsigned *done = counters + item.image;
+          const volatile unsigned *err = ctl + 1;
+          while (*done < (unsigned)im.tiles0) {
+            if (*err != 0u || global_ns() - t0 > wait_ns) {
+              ok = 0;
+              atomicExch(&ctl[1], 1u);
+              break;
+            }
+            __nanosleep(128);
           }
-          __nanosleep(128);
+          __threadfence();
+          if (ok) s_seen = item.image;
         }
-        __threadfence();
         s_ok = ok;
       }
       __syncthreads();
@@ -503,10 +556,10 @@ ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__
       const int kind = item.pass == 0 ? im.kind0 : im.kind1;
       if (kind == RAGGED_FAST_A)
         ragged_fast_a_item(im.s0, reinterpret_cast<const float *>(in) + im.in_off,
-                           reinterpret_cast<float *>(inter) + im.inter_off, item.tile, xs);
+                           reinterpret_cast<float *>(inter) + im.inter_off, item.tile, xs, prefetch);
       else if (kind == RAGGED_FAST_B)
         ragged_fast_b_item(reinterpret_cast<const float *>(inter) + im.inter_off,
-                           reinterpret_cast<float *>(out) + im.out_off, im.n, im.cs, item.tile, xs);
+                           reinterpret_cast<float *>(out) + im.out_off, im.n, im.cs, item.tile, xs, prefetch);
       if (kind != RAGGED_GENERIC) {
         __syncthreads();
         if (item.pass == 0 && im.s1 > 0 && threadIdx.x == 0) {
@@ -539,6 +592,7 @@ ragged_fwd_kernel(const T *__restrict__ in, T *__restrict__ out, T *__restrict__
         ragged_generic_item<T, false, true>(im.s1, a, t, smem_raw);
       }
     }
+    prefetch();
     __syncthreads();
     if (item.pass == 0 && im.s1 > 0 && threadIdx.x == 0) {
       __threadfence();

@@ -66,6 +66,14 @@ static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange
 
 __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
 
+// Called by every thread of a tile once, after its group-1 loads have been
+// issued and before the tile's first barrier (or at the start of a tile that
+// only stores zeros): a persistent caller fetches its next work item there,
+// where the fetch's latency overlaps the other warps' group-1 work.
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
 __device__ __forceinline__ float4 ld4_stream(const float *p) {
   return __ldcs(reinterpret_cast<const float4 *>(p));
 }
@@ -341,6 +349,73 @@ __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase
 }
 
 
+// Group 2's three stages (the fresh butterfly after the pre-shift).
+__device__ __forceinline__ void group2_stage_a(const float (&r)[8][8], float (&t0)[4][2][8]) {
+  // stage a: pairs (2P, 2P+1), shift p.
+#pragma unroll
+  for (int P = 0; P < 4; ++P) {
+    const float pv = __shfl_up_sync(FULL, r[2 * P + 1][7], 1);
+#pragma unroll
+    for (int k = 0; k < 8; k += 2)
+      add_rn2(r[2 * P][k], r[2 * P][k + 1], r[2 * P + 1][k], r[2 * P + 1][k + 1], t0[P][0][k], t0[P][0][k + 1]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
+  }
+}
+
+__device__ __forceinline__ void group2_stage_b(const float (&t0)[4][2][8], float (&t1)[2][4][8]) {
+  // stage b: combos (2Q, 2Q+1), li in {0,1}, shift li + p.
+#pragma unroll
+  for (int Q = 0; Q < 2; ++Q) {
+#pragma unroll
+    for (int li = 0; li < 2; ++li) {
+      float ext[10];  // ext[k + 2] = odd value at position k, k in [-2, 8)
+      ext[0] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][6], 1);
+      ext[1] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][7], 1);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ext[k + 2] = t0[2 * Q + 1][li][k];
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const int sh = li + p;
+        if (sh % 2 == 0) {
+#pragma unroll
+          for (int k = 0; k < 8; k += 2)
+            add_rn2(t0[2 * Q][li][k], t0[2 * Q][li][k + 1], ext[k + 2 - sh], ext[k + 3 - sh], t1[Q][2 * li + p][k],
+                    t1[Q][2 * li + p][k + 1]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) t1[Q][2 * li + p][k] = add_rn(t0[2 * Q][li][k], ext[k + 2 - sh]);
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void group2_stage_c(const float (&t1)[2][4][8], float (&out)[8][8]) {
+  // stage c: li in [0,4), shift li + p.
+#pragma unroll
+  for (int li = 0; li < 4; ++li) {
+    float ext[12];  // ext[k + 4] = odd value at position k, k in [-4, 8)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ext[k] = __shfl_up_sync(FULL, t1[1][li][4 + k], 1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) ext[k + 4] = t1[1][li][k];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const int sh = li + p;
+      if (sh % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; k += 2)
+          add_rn2(t1[0][li][k], t1[0][li][k + 1], ext[k + 4 - sh], ext[k + 5 - sh], out[2 * li + p][k],
+                  out[2 * li + p][k + 1]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) out[2 * li + p][k] = add_rn(t1[0][li][k], ext[k + 4 - sh]);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Group 2: stages 2-4 for angle L1 of group 1; lane owns 8 combos x 8
 // positions (block b).  Returns out[l][k], l = local angle (tile angle 8*L1 + l).
@@ -387,78 +462,24 @@ __device__ __forceinline__ void group2_compute(const float *xs, int b, bool acti
     for (int h = 0; h < 8; ++h)
 #pragma unroll
       for (int k = 0; k < 8; ++k) out[h][k] = r[h][k];
-    return;
-  }
-  // stage a: pairs (2P, 2P+1), shift p.
-  float t0[4][2][8];
+  } else {
+    float t0[4][2][8];
+    group2_stage_a(r, t0);
+    if constexpr (GS == 1) {
 #pragma unroll
-  for (int P = 0; P < 4; ++P) {
-    const float pv = __shfl_up_sync(FULL, r[2 * P + 1][7], 1);
+      for (int e = 0; e < 8; ++e)
 #pragma unroll
-    for (int k = 0; k < 8; k += 2)
-      add_rn2(r[2 * P][k], r[2 * P][k + 1], r[2 * P + 1][k], r[2 * P + 1][k + 1], t0[P][0][k], t0[P][0][k + 1]);
+        for (int k = 0; k < 8; ++k) out[e][k] = t0[e >> 1][e & 1][k];
+    } else {
+      float t1[2][4][8];
+      group2_stage_b(t0, t1);
+      if constexpr (GS == 2) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) t0[P][1][k] = add_rn(r[2 * P][k], k ? r[2 * P + 1][k - 1] : pv);
-  }
-  if constexpr (GS == 1) {
+        for (int e = 0; e < 8; ++e)
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-#pragma unroll
-      for (int k = 0; k < 8; ++k) out[e][k] = t0[e >> 1][e & 1][k];
-    return;
-  }
-  // stage b: combos (2Q, 2Q+1), li in {0,1}, shift li + p.
-  float t1[2][4][8];
-#pragma unroll
-  for (int Q = 0; Q < 2; ++Q) {
-#pragma unroll
-    for (int li = 0; li < 2; ++li) {
-      float ext[10];  // ext[k + 2] = odd value at position k, k in [-2, 8)
-      ext[0] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][6], 1);
-      ext[1] = __shfl_up_sync(FULL, t0[2 * Q + 1][li][7], 1);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) ext[k + 2] = t0[2 * Q + 1][li][k];
-#pragma unroll
-      for (int p = 0; p < 2; ++p) {
-        const int sh = li + p;
-        if (sh % 2 == 0) {
-#pragma unroll
-          for (int k = 0; k < 8; k += 2)
-            add_rn2(t0[2 * Q][li][k], t0[2 * Q][li][k + 1], ext[k + 2 - sh], ext[k + 3 - sh], t1[Q][2 * li + p][k],
-                    t1[Q][2 * li + p][k + 1]);
-        } else {
-#pragma unroll
-          for (int k = 0; k < 8; ++k) t1[Q][2 * li + p][k] = add_rn(t0[2 * Q][li][k], ext[k + 2 - sh]);
-        }
-      }
-    }
-  }
-  if constexpr (GS == 2) {
-#pragma unroll
-    for (int e = 0; e < 8; ++e)
-#pragma unroll
-      for (int k = 0; k < 8; ++k) out[e][k] = t1[e >> 2][e & 3][k];
-    return;
-  }
-  // stage c: li in [0,4), shift li + p.
-#pragma unroll
-  for (int li = 0; li < 4; ++li) {
-    float ext[12];  // ext[k + 4] = odd value at position k, k in [-4, 8)
-#pragma unroll
-    for (int k = 0; k < 4; ++k) ext[k] = __shfl_up_sync(FULL, t1[1][li][4 + k], 1);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) ext[k + 4] = t1[1][li][k];
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-      const int sh = li + p;
-      if (sh % 2 == 0) {
-#pragma unroll
-        for (int k = 0; k < 8; k += 2)
-          add_rn2(t1[0][li][k], t1[0][li][k + 1], ext[k + 4 - sh], ext[k + 5 - sh], out[2 * li + p][k],
-                  out[2 * li + p][k + 1]);
+          for (int k = 0; k < 8; ++k) out[e][k] = t1[e >> 2][e & 3][k];
       } else {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) out[2 * li + p][k] = add_rn(t1[0][li][k], ext[k + 4 - sh]);
+        group2_stage_c(t1, out);
       }
     }
   }
@@ -574,8 +595,9 @@ __device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q,
 // intermediate [q][g (32)][a (2^S)][CS].  FULL_SWEEP: every tile sweeps all
 // positions (a persistent loop around a sweep of run-time length spills; the
 // positions past the stored ones are computed and dropped).
-template <int S, bool FULL_SWEEP = false>
-__device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, int q, int R, int ct, float *xs) {
+template <int S, bool FULL_SWEEP = false, class Hook = NoHook>
+__device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, int q, int R, int ct, float *xs,
+                                            const Hook &hook = Hook()) {
   using P = PassA<S>;
   const int c0 = ct * W, tbase = c0 - HALO;
   const int pos = needed_positions(min(W, P::CS - c0));
@@ -585,6 +607,7 @@ __device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, 
   } else {
     group1_passA_cols<P::n>(img, q, R, tbase, pos, xs);
   }
+  hook();
   __syncthreads();
   float *inter_q = inter_img + (size_t)q * P::n * P::CS;
   switch ((threadIdx.x >> 5) & 3) {
@@ -600,9 +623,9 @@ __device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, 
 // [a (n/32)][cs], out_img = its (4, 2n-1, n) output.  LD: cache mode of the
 // intermediate's loads; FULL_SWEEP as for pass_a_tile (the live rows are
 // stored either way).
-template <int LD, bool FULL_SWEEP = false>
+template <int LD, bool FULL_SWEEP = false, class Hook = NoHook>
 __device__ __forceinline__ void pass_b_tile(const float *inter_img, float *out_img, int n, int cs, int q, int ap,
-                                            int ct, float *xs) {
+                                            int ct, float *xs, const Hook &hook = Hook()) {
   const int a_in = n / 32;
   const int c0 = ct * W, tbase = c0 - HALO;
   float *dst_q = out_img + (size_t)q * (2 * n - 1) * n;
@@ -613,6 +636,7 @@ __device__ __forceinline__ void pass_b_tile(const float *inter_img, float *out_i
   const int lim = min(2 * n - 1, n + 32 * ap + 31);
   const int live = min(W, lim - c0);
   if (live <= 0) {
+    hook();
     passB_store_tile(xs, dst_q, ap, c0, n, 0);
     return;
   }
@@ -635,6 +659,7 @@ __device__ __forceinline__ void pass_b_tile(const float *inter_img, float *out_i
       default: group1_passB<3, 0, LD>(src, ap, tbase, pos, xs, mstride, cs); break;
     }
   }
+  hook();
   __syncthreads();
   float out[8][8];
   group2_passB_compute(xs, live, out);
