@@ -428,20 +428,22 @@ template <int L1, int XL = 0, int GS = 3>
 __device__ __forceinline__ void group2_compute(const float *xs, int b, bool active,
                                                float (&out)[8][8]) {
   static_assert(GS >= 0 && GS <= 3, "group 2 runs 0 to 3 stages");
+  const int bl = active ? b : W / 8 - 1;
   float r[8][8];
 #pragma unroll
   for (int h = 0; h < 8; ++h) {
     const int hl = h & ((1 << GS) - 1);
     const int qh = (L1 * hl) >> 2, mh = (L1 * hl) & 3;
-    float4 B = make_float4(0.f, 0.f, 0.f, 0.f), Cc = B, A = B;
     const float *row = xs + xrow<XL>(h, L1) * RS;
-    if (active) {
-      B = *reinterpret_cast<const float4 *>(row + swz(8 + 2 * b - qh) * 4);
-      Cc = *reinterpret_cast<const float4 *>(row + swz(9 + 2 * b - qh) * 4);
-    }
-    // Lane 0 has no left neighbour: it reads the preceding chunk itself.
-    if (mh > 0 && (threadIdx.x & 31) == 0)
-      A = *reinterpret_cast<const float4 *>(row + swz(7 + 2 * b - qh) * 4);
+    // Every lane reads, without a branch: the two lanes past the tile (half 1,
+    // lanes 30-31) at the last block, in bounds (chunks <= 127 of 129); their
+    // values only travel to higher lanes by shuffle, so no stored lane sees them.
+    const float4 B = *reinterpret_cast<const float4 *>(row + swz(8 + 2 * bl - qh) * 4);
+    const float4 Cc = *reinterpret_cast<const float4 *>(row + swz(9 + 2 * bl - qh) * 4);
+    // Lane 0 has no left neighbour: it takes the preceding chunk, which every
+    // lane reads (chunk 5 - qh >= 0 at block -1).
+    float4 A = B;
+    if (mh > 0) A = *reinterpret_cast<const float4 *>(row + swz(7 + 2 * bl - qh) * 4);
     const float bv[4] = {B.x, B.y, B.z, B.w};
     const float cv[4] = {Cc.x, Cc.y, Cc.z, Cc.w};
     const float av[4] = {A.x, A.y, A.z, A.w};
