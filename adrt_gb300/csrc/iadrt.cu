@@ -115,6 +115,125 @@ iadrt_stage_kernel(const T *__restrict__ in, T *__restrict__ out, i64 planes, i6
   }
 }
 
+// The last five stages (s0 = L-5 .. L-1) in one sweep.  Across them the
+// chains form closed groups: output chains of level L with angles
+// [32A, 32A + 32) depend only on the level-s0 chains of angle A (its 32
+// sections), and at every level s0 + t in between the group's 32 chains sit
+// at chain indices 32A .. 32A + 31 (angle A 2^t + (lane >> (5-t)), section
+// lane mod 2^(5-t)).  One warp runs one group of one plane: it walks the rows
+// from R-1 down to 0 and, at each row, computes the five levels in order, each
+// lane one chain per level with the recurrence above (same operations, same
+// order).  A level reads the previous one at rows r, r + 1 and r + d, d = 1 +
+// col <= 16, so each level's last 17 rows stay in a shared-memory ring.  The
+// five intermediate levels never leave the SM: one read of the input and one
+// write of the output replace five of each.
+constexpr int kLast5Ring = 17;      // rows r .. r + 16
+constexpr int kLast5Prefetch = 8;   // input rows loaded ahead
+// Warps (groups) per CTA: the rings of a CTA stay under 48 KB of static
+// shared memory (44.9 KB for float32 x 4 warps, float64 x 2).
+template <typename T> constexpr int last5_warps() { return sizeof(T) == 4 ? 4 : 2; }
+
+// One row of the fused sweep for this lane: the five levels in order.  Both
+// recurrences read two values of the previous level: even chains E[r] and
+// O[r + 1], odd chains O[r + d] and E[r + d]; the lane's ring rows and
+// lanes are chosen by select, so the warp does not diverge between them.
+// EDGE: a row within 16 of the top (some operands lie past row R-1: the
+// reference's conditions apply); elsewhere every operand exists.
+template <typename T, bool EDGE>
+__device__ __forceinline__ void last5_row(T (*rg)[kLast5Ring][33], int r, int R, int slot, const int (&la)[5],
+                                          const int (&lb)[5], const int (&dd)[5], const bool (&odd)[5],
+                                          T (&prev)[5], T *dst_row, int lane) {
+  constexpr int H = kLast5Ring;
+  const int s1 = slot + 1 == H ? 0 : slot + 1;
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    int sd = slot + dd[t];
+    sd -= sd >= H ? H : 0;
+    const T x1 = rg[t][odd[t] ? sd : slot][la[t]];  // E[r] or O[r + d]
+    const T x2 = rg[t][odd[t] ? sd : s1][lb[t]];    // O[r + 1] or E[r + d]
+    T v;
+    if (!EDGE) {
+      v = add_rn(T(0), x1);
+      v = sub_rn(v, x2);
+      v = add_rn(v, prev[t]);
+    } else {
+      // even: v = (0 + E[r]); if r + 1 < R: v = v - O[r + 1] + prev
+      // odd:  v = 0; if r + d < R: v = (0 + O[r + d]) - E[r + d]; if r + 1 < R: v += prev
+      const bool in1 = r + 1 < R, ind = r + dd[t] < R;
+      const bool first = odd[t] ? ind : true, second = odd[t] ? ind : in1;
+      v = first ? add_rn(T(0), x1) : T(0);
+      if (second) v = sub_rn(v, x2);
+      if (in1) v = add_rn(v, prev[t]);
+    }
+    prev[t] = v;
+    if (t < 4) {
+      rg[t + 1][slot][lane] = v;
+      __syncwarp();
+    } else {
+      *dst_row = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * last5_warps<T>())
+iadrt_last5_kernel(const T *__restrict__ in, T *__restrict__ out, i64 groups, int n) {
+  constexpr int WPB = last5_warps<T>();
+  constexpr int H = kLast5Ring, LS = 33;  // ring row stride: lanes reading rows r and r + d hit distinct banks
+  __shared__ T ring[WPB][5][H][LS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const i64 g = blockIdx.x * (i64)WPB + w;
+  if (g >= groups) return;  // whole warps only: the sweep below synchronises within the warp
+  const int gpp = n >> 5;   // groups per plane
+  const i64 plane = g / gpp;
+  const int A = (int)(g - plane * gpp);
+  const int R = 2 * n - 1;
+  const T *src = in + plane * (i64)R * n + 32 * A + lane;
+  T *dst = out + plane * (i64)R * n + 32 * A + lane;
+  T(*rg)[H][LS] = ring[w];
+  // Per output level t + 1: parity, input lanes and lag of this lane's chain
+  // (la: the lane of the first operand, E for even chains, O for odd ones).
+  int la[5], lb[5], dd[5];
+  bool odd[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const int lam = lane >> (4 - t), col = lane & ((1 << (4 - t)) - 1);
+    const int e = ((lam >> 1) << (5 - t)) + 2 * col;
+    odd[t] = lam & 1;
+    la[t] = odd[t] ? e + 1 : e;
+    lb[t] = odd[t] ? e : e + 1;
+    dd[t] = 1 + col;
+  }
+  T prev[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) prev[t] = T(0);
+  constexpr int U = kLast5Prefetch;
+  T q[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int r = R - 1 - u;
+    q[u] = r >= 0 ? __ldg(src + (size_t)r * n) : T(0);
+  }
+  int slot = (R - 1) % H;  // ring slot of row r
+  for (int row0 = R - 1; row0 >= 0; row0 -= U) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int r = row0 - u;
+      if (r >= 0) {  // warp-uniform
+        rg[0][slot][lane] = q[u];
+        __syncwarp();
+        if (r >= R - 16)
+          last5_row<T, true>(rg, r, R, slot, la, lb, dd, odd, prev, dst + (size_t)r * n, lane);
+        else
+          last5_row<T, false>(rg, r, R, slot, la, lb, dd, odd, prev, dst + (size_t)r * n, lane);
+        slot = slot == 0 ? H - 1 : slot - 1;
+      }
+      const int rn = r - U;
+      q[u] = rn >= 0 ? __ldg(src + (size_t)rn * n) : T(0);
+    }
+  }
+}
+
 template <typename T>
 __global__ void copy_kernel(const T *__restrict__ in, T *__restrict__ out, i64 total) {
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < total;
@@ -149,7 +268,9 @@ int iadrt_launch(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
   const int bs = threads >= (i64)152 * 4 * 128 ? 128 : 32;
   const unsigned grid = (unsigned)((threads + bs - 1) / bs);
   constexpr int U_DEEP = sizeof(T) == 4 ? 32 : 16;
-  for (int s = 0; s < L; ++s) {
+  // n >= 32: the first L-5 stages one kernel each, the last five fused.
+  const int single = L >= 5 ? L - 5 : L;
+  for (int s = 0; s < single; ++s) {
     T *dst = (s == L - 1) ? out : bufs[s & 1];
     if (n >= 1024)
       iadrt_stage_kernel<T, U_DEEP><<<grid, bs, 0, st>>>(src, dst, planes, n, s);
@@ -158,6 +279,13 @@ int iadrt_launch(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
     const int rc = launch_status();
     if (rc) return rc;
     src = dst;
+  }
+  if (L >= 5) {
+    const i64 groups = planes * (n >> 5);
+    constexpr int WPB = last5_warps<T>();
+    const unsigned g5 = (unsigned)((groups + WPB - 1) / WPB);
+    iadrt_last5_kernel<T><<<g5, 32 * WPB, 0, st>>>(src, out, groups, (int)n);
+    return launch_status();
   }
   return ADRT_GB300_OK;
 }
