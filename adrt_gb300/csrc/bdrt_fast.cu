@@ -45,6 +45,9 @@ constexpr int NCH = 128;           // exchange chunks per row
 constexpr int RS = 4 * (NCH + 1);  // exchange row stride in floats (odd chunk count)
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 constexpr unsigned FULL = 0xffffffffu;
+// Pass 1 runs at n = 1024 only: its geometry is compile-time (offsets fold
+// into the loads' and stores' immediate fields).
+constexpr int N1 = 1024, C1 = 2 * N1 - 1, CS1 = (C1 + 7) / 8 * 8;  // CS1: the padded buffer row
 static_assert(TWI * 32 <= 32 * RS && W * 32 <= 32 * RS, "stagings fit in the exchange buffer");
 
 __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
@@ -146,12 +149,13 @@ __device__ __forceinline__ void put_exchange_t(float *xs, int b, bool wr, const 
     float v[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = k + mh < 8 ? t2[h][(k + mh) & 7] : nx[(k + mh - 8) & 3];
-    if (wr) {
-      float *row = xs + (h * 4 + L1) * RS;
-      const int x0 = 2 * b - qh;
-      if (x0 >= 0) *reinterpret_cast<float4 *>(row + swz(x0) * 4) = make_float4(v[0], v[1], v[2], v[3]);
-      if (x0 + 1 >= 0) *reinterpret_cast<float4 *>(row + swz(x0 + 1) * 4) = make_float4(v[4], v[5], v[6], v[7]);
-    }
+    // A chunk this lane does not write goes to the row's padding chunk
+    // (NCH), which no read touches: the stores need no branch.
+    float *row = xs + (h * 4 + L1) * RS;
+    const int x0 = 2 * b - qh;
+    const int c0w = wr && x0 >= 0 ? swz(x0) : NCH, c1w = wr && x0 + 1 >= 0 ? swz(x0 + 1) : NCH;
+    *reinterpret_cast<float4 *>(row + c0w * 4) = make_float4(v[0], v[1], v[2], v[3]);
+    *reinterpret_cast<float4 *>(row + c1w * 4) = make_float4(v[4], v[5], v[6], v[7]);
   }
 }
 
@@ -230,19 +234,21 @@ __device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&
 // offset); output: bdrt buffer rows (a', member i) at reference offset
 // u - a' i, row stride cs.  A4 = a' mod 4 fixes each member's sub-chunk shift.
 template <int A4>
-__device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *rows_ap, int ap, int c0, int cs,
-                                            int C, int h) {
+__device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *rows_ap, int ap, int c0, int h) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int it = 0; it < 4; ++it) {
-    const int ch = 31 * it + lane;
+  for (int m = 0; m < 4; ++m) {
+    const int i = 4 * h + m;
+    const int D = ap * i;
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int mi = (A4 * m) & 3;  // == D & 3
+    float *row = rows_ap + i * CS1;
+    // Chunk X = ch + c0/4 - D/4 of the member's row; stored when it holds
+    // stored tile positions and lies in [0, 2n-1): X in [0, ceil(C/4)).
+    const int X0 = lane + (c0 >> 2) - (D >> 2);
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      constexpr int dummy = 0;
-      (void)dummy;
-      const int i = 4 * h + m;
-      const int D = ap * i;
-      const int mi = (A4 * m) & 3;  // == D & 3
+    for (int it = 0; it < 4; ++it) {
       // The chunk to the right: lane + 1's, except for lane 30, whose right
       // neighbour (lane 31) only seeds; that chunk is lane 0's next sweep.
       float nx[4];
@@ -256,17 +262,19 @@ __device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *ro
       float v[4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) v[k] = k + mi < 4 ? o[it][m][(k + mi) & 3] : nx[(k + mi - 4) & 3];
-      const int X = ch + (c0 >> 2) - (D >> 2);
-      if (lane < 31 && 4 * ch + mi < W && X >= 0 && 4 * X < C)
-        *reinterpret_cast<float4 *>(rows_ap + (size_t)i * cs + 4 * X) = make_float4(v[0], v[1], v[2], v[3]);
+      const int X = X0 + 31 * it;
+      // lane < 31 and 4 ch + mi < W, ch = 31 it + lane
+      const int lane_lim = min(31, (W - mi + 3) / 4 - 31 * it);
+      if (lane < lane_lim && (unsigned)X < (unsigned)((C1 + 3) / 4))
+        *reinterpret_cast<float4 *>(row + 4 * X) = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 }
 
-__global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ in, float *__restrict__ buf, int n,
-                                                      int cs, int need) {
+__global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ in, float *__restrict__ buf,
+                                                      int need) {
   extern __shared__ __align__(16) float xs[];
-  const int C = 2 * n - 1;
+  constexpr int n = N1, C = C1;
   const int c0 = (int)blockIdx.x * W;
   const int bq = (int)blockIdx.y;  // image * 4 + quadrant
   const int ap = (int)blockIdx.z;
@@ -318,12 +326,12 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
   float o[4][4][4];
 #pragma unroll
   for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + (threadIdx.x & 31), o[it], edge, kc, ap);
-  float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * cs;
+  float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * CS1;
   switch (ap & 3) {
-    case 0: pass1_store<0>(o, rows_ap, ap, c0, cs, C, h); break;
-    case 1: pass1_store<1>(o, rows_ap, ap, c0, cs, C, h); break;
-    case 2: pass1_store<2>(o, rows_ap, ap, c0, cs, C, h); break;
-    default: pass1_store<3>(o, rows_ap, ap, c0, cs, C, h); break;
+    case 0: pass1_store<0>(o, rows_ap, ap, c0, h); break;
+    case 1: pass1_store<1>(o, rows_ap, ap, c0, h); break;
+    case 2: pass1_store<2>(o, rows_ap, ap, c0, h); break;
+    default: pass1_store<3>(o, rows_ap, ap, c0, h); break;
   }
 }
 
@@ -331,10 +339,11 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
 // Input: bdrt buffer rows (angle l, section r) for l < 32, row stride cs;
 // output: (4, 2n-1, n) sections 32 r .. 32 r + 31 (128 bytes per offset),
 // staged in shared memory (chunk h of row p at chunk h ^ ((p >> 2) & 7)).
-__global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ buf, float *__restrict__ out, int n,
-                                                      int cs, int need) {
+template <int NN>
+__global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ buf, float *__restrict__ out,
+                                                      int need) {
   extern __shared__ __align__(16) float xs[];
-  const int C = 2 * n - 1;
+  constexpr int n = NN, C = 2 * n - 1, cs = (C + 7) / 8 * 8;
   const int c0 = (int)blockIdx.x * W;
   if (c0 >= need) return;
   const int bq = (int)blockIdx.y;
@@ -377,16 +386,18 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
 #pragma unroll
   for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + lane, o[it], edge, kc, 0);
   __syncthreads();  // the output staging overlays the exchange
+  // Chunks past the tile (and lane 31's, a seed) go to a spare slot past the
+  // staged rows (float W * 32), which no read touches: no branch.
+  static_assert(W * 32 + 4 <= 32 * RS, "spare staging slot inside the buffer");
 #pragma unroll
   for (int it = 0; it < 4; ++it) {
     const int ch = 31 * it + lane;
-    if (lane < 31 && ch < W / 4) {
+    const bool st = lane < 31 && ch < W / 4;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int p = 4 * ch + k;
-        *reinterpret_cast<float4 *>(xs + p * 32 + 4 * (h ^ (ch & 7))) =
-            make_float4(o[it][0][k], o[it][1][k], o[it][2][k], o[it][3][k]);
-      }
+    for (int k = 0; k < 4; ++k) {
+      const int p = 4 * ch + k;
+      *reinterpret_cast<float4 *>(xs + (st ? p * 32 + 4 * (h ^ (ch & 7)) : W * 32)) =
+          make_float4(o[it][0][k], o[it][1][k], o[it][2][k], o[it][3][k]);
     }
   }
   __syncthreads();
@@ -417,31 +428,43 @@ int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 n
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)bfast::pass1_kernel, bfast::SMEM, configured)) return rc;
   const int tiles = pass_tiles(n, true);
-  if (n != 1024) return ADRT_GB300_ERR_SHAPE;
+  if (n != bfast::N1 || cs != bfast::CS1) return ADRT_GB300_ERR_SHAPE;
   // Grid y counts (image, quadrant) pairs: launches of at most 16383 images.
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
     const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), 32);
     bfast::pass1_kernel<<<grid, bfast::NT, bfast::SMEM, st>>>(in + b0 * 4 * (2 * n - 1) * n, buf + b0 * 4 * n * cs,
-                                                                (int)n, (int)cs, (int)need);
+                                                                (int)need);
     if (const int rc = launch_status()) return rc;
   }
   return ADRT_GB300_OK;
 }
 
-int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+template <int NN>
+static int launch_pass2(const float *buf, float *out, i64 batch, i64 need, cudaStream_t st) {
+  constexpr i64 n = NN, cs = (2 * NN - 1 + 7) / 8 * 8;
   static std::atomic<unsigned long long> configured{0};
-  if (const int rc = smem_limit_once((const void *)bfast::pass2_kernel, bfast::SMEM, configured)) return rc;
+  if (const int rc = smem_limit_once((const void *)bfast::pass2_kernel<NN>, bfast::SMEM, configured)) return rc;
   const int tiles = pass_tiles(n, false);
-  if (n < 256 || n > 1024) return ADRT_GB300_ERR_SHAPE;
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
     const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(n / 32));
-    bfast::pass2_kernel<<<grid, bfast::NT, bfast::SMEM, st>>>(buf + b0 * 4 * n * cs, out + b0 * 4 * (2 * n - 1) * n,
-                                                                (int)n, (int)cs, (int)need);
+    bfast::pass2_kernel<NN><<<grid, bfast::NT, bfast::SMEM, st>>>(buf + b0 * 4 * n * cs,
+                                                                    out + b0 * 4 * (2 * n - 1) * n, (int)need);
     if (const int rc = launch_status()) return rc;
   }
   return ADRT_GB300_OK;
+}
+
+// The bdrt buffer's rows are padded to 8 floats (cs = (2n - 1 + 7) / 8 * 8).
+int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+  if (cs != (2 * n - 1 + 7) / 8 * 8) return ADRT_GB300_ERR_SHAPE;
+  switch (n) {
+    case 256: return launch_pass2<256>(buf, out, batch, need, st);
+    case 512: return launch_pass2<512>(buf, out, batch, need, st);
+    case 1024: return launch_pass2<1024>(buf, out, batch, need, st);
+  }
+  return ADRT_GB300_ERR_SHAPE;
 }
 
 }  // namespace adrtg
