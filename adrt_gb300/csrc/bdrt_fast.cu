@@ -54,6 +54,17 @@ __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
 
 __device__ __forceinline__ float4 ld4_cs(const float *p) { return __ldcs(reinterpret_cast<const float4 *>(p)); }
 
+// Streaming 16-byte load under a predicate: `fill` where it is false, with
+// no memory access (predicated in PTX, so the choice costs no branch).
+__device__ __forceinline__ float4 ld4_cs_if(const float *p, bool pred, float4 fill) {
+  float4 v;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\tmov.b32 %0, %6;\n\tmov.b32 %1, %7;\n\t"
+      "mov.b32 %2, %8;\n\tmov.b32 %3, %9;\n\t@q ld.global.cs.v4.f32 {%0, %1, %2, %3}, [%4];\n\t}"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p), "r"((unsigned)pred), "f"(fill.x), "f"(fill.y), "f"(fill.z), "f"(fill.w));
+  return v;
+}
+
 // Right output of one undone stage over 8 positions: d[k] = A[k + s] +
 // B[k + s + 1], where positions 8.. come from lane + 1.
 template <int S>
@@ -293,8 +304,8 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
     for (int i = 0; i < 16; ++i) {
       const int r = r0 + 32 * i;
       if (r < TWI) {
-        if (r < kc) v[i] = ld4_cs(src + (size_t)(c0 + r) * n + 4 * j);
-        else v[i] = r == kc ? make_float4(0.f, -0.f, 0.f, -0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float z = r == kc ? -0.f : 0.f;
+        v[i] = ld4_cs_if(src + (size_t)(c0 + r) * n + 4 * j, r < kc, make_float4(0.f, z, 0.f, z));
       }
     }
 #pragma unroll
@@ -361,9 +372,8 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
 #pragma unroll
   for (int l3 = 0; l3 < 8; ++l3) {
     const float *p = src + (size_t)l3 * R * cs;
-    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
-    if (e0 < kc) v0 = ld4_cs(p);
-    if (e0 + 4 < kc) v1 = ld4_cs(p + 4);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 v0 = ld4_cs_if(p, e0 < kc, zero), v1 = ld4_cs_if(p + 4, e0 + 4 < kc, zero);
     a[l3][0] = v0.x; a[l3][1] = v0.y; a[l3][2] = v0.z; a[l3][3] = v0.w;
     a[l3][4] = v1.x; a[l3][5] = v1.y; a[l3][6] = v1.z; a[l3][7] = v1.w;
   }
@@ -404,13 +414,12 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
   const int p0 = threadIdx.x >> 3, j = threadIdx.x & 7;
   float *dst = out + (size_t)bq * C * n + 32 * r + 4 * j;
   const int lim = min(min(C, need) - c0, W);
+  // Rows p < W are inside the staging: read them all, store the live ones.
 #pragma unroll
   for (int i = 0; i < W / 32; ++i) {
     const int p = p0 + 32 * i;
-    if (p < lim) {
-      const float4 v = *reinterpret_cast<const float4 *>(xs + p * 32 + 4 * (j ^ ((p >> 2) & 7)));
-      __stcs(reinterpret_cast<float4 *>(dst + (size_t)(c0 + p) * n), v);
-    }
+    const float4 v = *reinterpret_cast<const float4 *>(xs + p * 32 + 4 * (j ^ ((p >> 2) & 7)));
+    if (p < lim) __stcs(reinterpret_cast<float4 *>(dst + (size_t)(c0 + p) * n), v);
   }
 }
 
