@@ -303,20 +303,30 @@ __device__ __forceinline__ void group1_passB(const float *src, int ap, int tbase
   constexpr int IT = NCH / 32;
   const int nit = NIT ? NIT : sweep_iters(pos);
   float4 raw[IT + 1][4];
+  // Member j's sweep starts at gb_j = tbase - 4 floor(a' j / 4), which falls
+  // with j: when the warp's first member ends inside the row and its last
+  // starts past the first chunk, every load of the warp is inside (one
+  // warp-uniform branch for all four members).
+  const int gb_hi = tbase - 4 * ((ap * (4 * mq)) >> 2), gb_lo = tbase - 4 * ((ap * (4 * mq + 3)) >> 2);
+  if (gb_lo >= 4 && gb_hi + 128 * nit <= cs) {
 #pragma unroll
-  for (int jj = 0; jj < 4; ++jj) {
-    const int j = 4 * mq + jj;
-    const float *row = src + (size_t)j * mstride;
-    const int gb = tbase - 4 * ((ap * j) >> 2);
-    if (gb >= 4 && gb + 128 * nit <= cs) {
-      // the whole sweep lies inside the row: no fill values (warp-uniform)
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = 4 * mq + jj;
+      const float *row = src + (size_t)j * mstride;
+      const int gb = tbase - 4 * ((ap * j) >> 2);
 #pragma unroll
       for (int it = 0; it <= IT; ++it) {
         if (it > nit) break;
         const int g0 = it == 0 ? gb - 4 : gb + 4 * ((it - 1) * 32 + lane);
         raw[it][jj] = LD == LD_CG ? __ldcg(reinterpret_cast<const float4 *>(row + g0)) : ld4_stream(row + g0);
       }
-    } else {
+    }
+  } else {
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = 4 * mq + jj;
+      const float *row = src + (size_t)j * mstride;
+      const int gb = tbase - 4 * ((ap * j) >> 2);
 #pragma unroll
       for (int it = 0; it <= IT; ++it) {
         if (it > nit) break;
