@@ -438,12 +438,18 @@ __device__ __noinline__ void ragged_generic_item(int S, const FwdPassArgs a, i64
 
 // Register first pass of n = 32 * 2^S: item t = (quadrant, 32-row block R,
 // column tile), column tile fastest.
+// The sweep length is fixed per column tile at compile time: every tile but
+// the last is full; the last sweeps only its own iterations.
 template <int S, class Hook>
 __device__ __forceinline__ void ragged_fast_a_tile(const float *img, float *inter_img, int t, float *xs,
                                                    const Hook &hook) {
   using P = fast::PassA<S>;
-  fast::pass_a_tile<S, true>(img, inter_img, t / (P::TILES * (P::n / 32)), (t / P::TILES) % (P::n / 32),
-                             t % P::TILES, xs, hook);
+  constexpr int last = P::TILES - 1;
+  const int q = t / (P::TILES * (P::n / 32)), R = (t / P::TILES) % (P::n / 32), ct = t % P::TILES;
+  if (ct == last)
+    fast::pass_a_tile<S, fast::pass_a_nit<S>(last)>(img, inter_img, q, R, ct, xs, hook);
+  else
+    fast::pass_a_tile<S, fast::NCH / 32>(img, inter_img, q, R, ct, xs, hook);
 }
 
 template <class Hook>

@@ -61,6 +61,15 @@ struct PassA {
   static constexpr int TILES = (CS + W - 1) / W;            // 3, 2, 1, 1
   static constexpr int GS = S - 2;                          // stages of group 2
 };
+
+// Sweep iterations pass A's column tile ct needs for n = 32 * 2^S (the
+// compile-time form of sweep_iters(needed_positions(...))).
+template <int S>
+constexpr int pass_a_nit(int ct) {
+  const int live = PassA<S>::CS - ct * W < W ? PassA<S>::CS - ct * W : W;
+  const int it = (((live + 7) & ~7) + HALO + 127) >> 7;
+  return it < NCH / 32 ? it : NCH / 32;
+}
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 static_assert(W * 32 <= 32 * RS, "pass B output staging must fit in the exchange buffer");
 
@@ -604,17 +613,19 @@ __device__ __forceinline__ void passB_store_tile(const float *ost, float *dst_q,
 
 // One pass-A tile (n = 32 * 2^S): quadrant q, rows (or columns) 32 R ..
 // 32 R + 31, column tile ct of one image; inter_img = that image's
-// intermediate [q][g (32)][a (2^S)][CS].  FULL_SWEEP: every tile sweeps all
-// positions (a persistent loop around a sweep of run-time length spills; the
-// positions past the stored ones are computed and dropped).
-template <int S, bool FULL_SWEEP = false, class Hook = NoHook>
+// intermediate [q][g (32)][a (2^S)][CS].  NIT: the row-quadrant sweep length
+// when the caller fixes it at compile time (a persistent loop around a sweep
+// of run-time length spills), at least the tile's own (`pass_a_nit`);
+// 0: full tiles sweep all four iterations, others their own run-time count.
+template <int S, int NIT = 0, class Hook = NoHook>
 __device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, int q, int R, int ct, float *xs,
                                             const Hook &hook = Hook()) {
   using P = PassA<S>;
   const int c0 = ct * W, tbase = c0 - HALO;
   const int pos = needed_positions(min(W, P::CS - c0));
   if (q == 0 || q == 3) {
-    if (FULL_SWEEP || pos == TW) group1_passA_rows<P::n, NCH / 32>(img, q, R, tbase, pos, xs);
+    if constexpr (NIT > 0) group1_passA_rows<P::n, NIT>(img, q, R, tbase, pos, xs);
+    else if (pos == TW) group1_passA_rows<P::n, NCH / 32>(img, q, R, tbase, pos, xs);
     else group1_passA_rows<P::n>(img, q, R, tbase, pos, xs);
   } else {
     group1_passA_cols<P::n>(img, q, R, tbase, pos, xs);

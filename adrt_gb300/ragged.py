@@ -26,19 +26,22 @@ __all__ = ["adrt_ragged", "RaggedPlan", "iadrt_ragged", "iadrt_fmg_ragged"]
 def _sizes_array(images):
     if not isinstance(images, (list, tuple)) or not images:
         raise TypeError("images must be a non-empty list of CUDA tensors")
+    if not all(isinstance(im, torch.Tensor) for im in images):
+        raise TypeError("images must be CUDA tensors")
     dt, dev = images[0].dtype, images[0].device
-    sizes = []
-    for im in images:
-        if not (isinstance(im, torch.Tensor) and im.is_cuda):
+    if not dev.type == "cuda" or any(im.device != dev for im in images):
+        if not all(im.is_cuda for im in images):
             raise TypeError("images must be CUDA tensors")
-        if im.ndim != 2 or im.shape[0] != im.shape[1] or not is_pow2(int(im.shape[0])):
+        raise ValueError("all images must share dtype and device")
+    if any(im.dtype != dt for im in images):
+        raise ValueError("all images must share dtype and device")
+    shapes = [im.shape for im in images]
+    for sh in shapes:
+        if len(sh) != 2 or sh[0] != sh[1] or not is_pow2(int(sh[0])):
             raise ValueError("each image must be square with a power of two shape")
-        if im.shape[0] > 1024:
+        if sh[0] > 1024:
             raise ValueError("ragged batches take sides up to 1024")
-        if im.dtype != dt or im.device != dev:
-            raise ValueError("all images must share dtype and device")
-        sizes.append(int(im.shape[0]))
-    return np.asarray(sizes, dtype=np.int64), dt, dev
+    return np.fromiter((sh[0] for sh in shapes), dtype=np.int64, count=len(shapes)), dt, dev
 
 
 def _launch(images, wait_ns=0, starve_image=-1):
@@ -84,7 +87,7 @@ class RaggedPlan:
         self.out = torch.empty(sum(self.out_lengths), dtype=dtype, device=self.device)
 
     def packed_input(self, images):
-        return torch.cat([im.contiguous().reshape(-1) for im in images])
+        return torch.cat([im.reshape(-1) for im in images])
 
     def launch(self, packed, wait_ns=0, starve_image=-1):
         if not (isinstance(packed, torch.Tensor) and packed.device == self.out.device
@@ -104,11 +107,7 @@ class RaggedPlan:
                                                     self.code, stream)
 
     def views(self):
-        views, off = [], 0
-        for n, k in zip(self.sizes, self.out_lengths):
-            views.append(self.out[off:off + k].view(4, 2 * int(n) - 1, int(n)))
-            off += k
-        return views
+        return [t.view(4, 2 * n - 1, n) for t, n in zip(self.out.split(self.out_lengths), self.sizes.tolist())]
 
 
 def iadrt_ragged(arrays):
