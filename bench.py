@@ -751,13 +751,13 @@ def main():
             warm_ms.append(round(dt * 1e3, 1))
             if i >= 3 and max(warm_ms[-3:]) <= 1.1 * min(warm_ms[-3:]):
                 break
-        # Three timed windows of e2e_steps calls each; the line reports the
-        # best window and keeps every window and call.  The host is shared
-        # with the other GPUs' jobs: single device-to-host copies have taken
-        # 4x their usual time (180-210 ms among 46 ms calls) with nothing in
-        # this process changing.
+        # Five timed windows of e2e_steps calls each (about 2.5 s in all);
+        # the line reports the best window and keeps every window and call.
+        # The host is shared with the other GPUs' jobs: device-to-host copies
+        # have taken 2-4x their usual time (110-210 ms among 46 ms calls) in
+        # stretches of a few seconds, with nothing in this process changing.
         windows, call_ms = [], []
-        for _w in range(3):
+        for _w in range(5):
             gc.collect()
             gc.disable()
             barrier()
@@ -784,7 +784,7 @@ def main():
             "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
             "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
             "windows_img_s": [world * B * args.e2e_steps / w for w in windows],
-            "window": f"best of 3 windows of {args.e2e_steps} calls",
+            "window": f"best of 5 windows of {args.e2e_steps} calls",
             "warmup_call_ms": warm_ms,
             "call_ms": call_ms,
             "host_mem_gb": _host_mem_gb(),
