@@ -821,9 +821,16 @@ def main():
         yi = yd[:64].contiguous()
         del yd
         inv, t = dev_time(lambda: adrt.iadrt(yi), ks)
+        # The inverse's stages are serial recurrences over whole rows: each of
+        # the first L-5 stages reads and writes the whole (4, 2n-1, n) array
+        # (one kernel per stage), the last five run fused (one read, one write).
+        passes = max(n.bit_length() - 1 - 5, 0) + 1
         extras["iadrt"] = {"workload": f"iadrt of 64 x (4, {2 * n - 1}, {n}) float32", "img_s": 64 / t,
                            "roofline": roof(64 / t, 2 * bytes_per_image_bdrt(n, 4)),
-                           "bound_note": "serial chains of 2n-1 dependent adds per stage (latency)"}
+                           "roofline_stage_traffic": roof(64 / t, passes * 2 * bytes_per_image_bdrt(n, 4)),
+                           "bound_note": (f"{passes} passes over the array (the first L-5 stages one kernel each, "
+                                          "the last five fused), each reading and writing it once: "
+                                          "roofline_stage_traffic counts those bytes")}
         del inv, yi
         x64 = x[:64].double()
         y64, t64 = dev_time(lambda: adrt.adrt(x64), ks)
