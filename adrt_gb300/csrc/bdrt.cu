@@ -238,24 +238,24 @@ static int bwd_dispatch(int S, bool first, bool last, const BwdPassArgs &a, cuda
   return bwd_dispatch_S<T, false, false>(S, a, st);
 }
 
-// Register-level passes (bdrt_fast.cu), float32, 256 <= n <= 1024: the last
-// bdrt pass (forward stages 0..4) for every such n, the first one (stages
-// 5..9) at n = 1024.
+// Register-level passes (bdrt_fast.cu), float32, 128 <= n <= 1024: the first
+// bdrt pass undoes forward stages L-1 .. L-5, the second L-6 .. 0.
 int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
 int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st);
 
 static bool bwd_fast_eligible(i64 n, size_t elem) {
-  if (elem != 4 || n < 256 || n > 1024 || !is_pow2(n)) return false;
+  if (elem != 4 || n < 128 || n > 1024 || !is_pow2(n)) return false;
   const TuneConfig tc = tune_lookup(ADRT_GB300_OP_BDRT, ADRT_GB300_F32, n);
   return tc.use_fast != 0 && (tc.max_fused == 0 || tc.max_fused == 5);
 }
 
-// Pass plan: the fast path undoes forward stages 0..4 in its own last pass
-// (sizes[0] = 5) and the remaining L-5 in the first.
+// Pass plan: the fast path splits the forward's stages as its forward does,
+// [0, L-5) and [L-5, L): the first bdrt pass undoes the last five stages, the
+// second the first L-5.
 static int plan_bwd(i64 n, size_t elem, int *sizes) {
   if (bwd_fast_eligible(n, elem)) {
-    sizes[0] = 5;
-    sizes[1] = num_iters(n) - 5;
+    sizes[0] = num_iters(n) - 5;
+    sizes[1] = 5;
     return 2;
   }
   return plan_passes_bwd(n, elem, sizes);
@@ -336,7 +336,7 @@ int bdrt_forward(const T *in, T *out, i64 batch, i64 n, void *ws, size_t ws_byte
       int rc = ADRT_GB300_OK;
       bool done = false;
       if constexpr (sizeof(T) == 4) {
-        if (fast && (last || n == 1024)) {
+        if (fast) {
           rc = last ? bdrt_fast_pass2(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,
                                       a.c_need, st)
                     : bdrt_fast_pass1(static_cast<const float *>(src), static_cast<float *>(dst), nb, n, cs,

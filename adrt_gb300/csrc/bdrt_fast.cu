@@ -45,9 +45,16 @@ constexpr int NCH = 128;           // exchange chunks per row
 constexpr int RS = 4 * (NCH + 1);  // exchange row stride in floats (odd chunk count)
 constexpr size_t SMEM = sizeof(float) * 32 * RS;
 constexpr unsigned FULL = 0xffffffffu;
-// Pass 1 runs at n = 1024 only: its geometry is compile-time (offsets fold
-// into the loads' and stores' immediate fields).
-constexpr int N1 = 1024, C1 = 2 * N1 - 1, CS1 = (C1 + 7) / 8 * 8;  // CS1: the padded buffer row
+// Both passes are instantiated per n (128 .. 1024): their geometry is
+// compile-time (offsets fold into the loads' and stores' immediate fields).
+// cs: the bdrt buffer's row, 2n - 1 padded to 8 floats.
+template <int NN>
+struct Geo {
+  static constexpr int n = NN, C = 2 * NN - 1, cs = (C + 7) / 8 * 8;
+  static constexpr int S = NN == 1024 ? 5 : NN == 512 ? 4 : NN == 256 ? 3 : 2;  // stages of pass 2
+  static constexpr int GS = S - 2;                                                // of them in group 2t
+  static_assert(NN == (32 << S), "n = 128, 256, 512 or 1024");
+};
 static_assert(TWI * 32 <= 32 * RS && W * 32 <= 32 * RS, "stagings fit in the exchange buffer");
 
 __device__ __forceinline__ int swz(int ch) { return ch ^ ((ch >> 3) & 1); }
@@ -101,7 +108,8 @@ __device__ __forceinline__ void neg0_at(float (&v)[K], int f_minus_base) {
 // 2n-1: fresh position kc + m (2^J a' + 2^(J-2) L1) for combo m at level J,
 // kc = 2n-1 - c0; base = 8 b.
 template <int L1>
-__device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8], bool edge, int kc, int ap, int base) {
+__device__ __forceinline__ void group2t_three(float (&a)[8][8], float (&t2)[8][8], bool edge, int kc, int ap,
+                                              int base) {
   float t4[2][4][8];
   left8(a[0], a[1], t4[0][0]);
   right8<0>(a[0], a[1], t4[1][0]);
@@ -142,17 +150,64 @@ __device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8], boo
     }
 }
 
+// GS < 3 (a pass of S = GS + 2 stages, n = 32 * 2^S): the lane's 8 rows form
+// 8 >> GS sets of 2^GS angle rows (one set per section), each undone by GS
+// stages: the last GS steps of the three-stage case, with set s in place of
+// the level-(GS+2) combo bits.  Combo h = 2^GS s + (bits of this pass); its
+// frame shift is L1 (h mod 2^GS), and a combo's level-J position in the edge
+// rule counts only this pass's bits.
+template <int L1, int GS>
+__device__ __forceinline__ void group2t(float (&a)[8][8], float (&t2)[8][8], bool edge, int kc, int ap, int base) {
+  static_assert(GS >= 0 && GS <= 3, "group 2t undoes 0 to 3 stages");
+  if constexpr (GS == 0) {
+#pragma unroll
+    for (int h = 0; h < 8; ++h)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) t2[h][k] = a[h][k];
+  } else if constexpr (GS == 1) {
+#pragma unroll
+    for (int st = 0; st < 4; ++st) {
+      left8(a[2 * st], a[2 * st + 1], t2[2 * st]);
+      right8<0>(a[2 * st], a[2 * st + 1], t2[2 * st + 1]);
+    }
+  } else if constexpr (GS == 2) {
+    float t3[2][2][2][8];
+#pragma unroll
+    for (int st = 0; st < 2; ++st) {
+      left8(a[4 * st], a[4 * st + 1], t3[st][0][0]);
+      right8<0>(a[4 * st], a[4 * st + 1], t3[st][1][0]);
+      left8(a[4 * st + 2], a[4 * st + 3], t3[st][0][1]);
+      right8<1>(a[4 * st + 2], a[4 * st + 3], t3[st][1][1]);
+    }
+    if (edge) {
+#pragma unroll
+      for (int st = 0; st < 2; ++st)
+#pragma unroll
+        for (int c3 = 0; c3 < 2; ++c3) neg0_at(t3[st][c3][1], kc + c3 * (8 * ap + 2 * L1) - base);
+    }
+#pragma unroll
+    for (int st = 0; st < 2; ++st)
+#pragma unroll
+      for (int c3 = 0; c3 < 2; ++c3) {
+        left8(t3[st][c3][0], t3[st][c3][1], t2[4 * st + 2 * c3]);
+        right8<0>(t3[st][c3][0], t3[st][c3][1], t2[4 * st + 2 * c3 + 1]);
+      }
+  } else {
+    group2t_three<L1>(a, t2, edge, kc, ap, base);
+  }
+}
+
 // Writes combo h of angle L1 back to its tile positions: fresh position
-// 8b + k is tile position 8b + k - L1 h.  Lanes 30 and 31 write nothing (31
+// 8b + k is tile position 8b + k - L1 h (L1 (h mod 2^GS) for GS < 3).  Lanes 30 and 31 write nothing (31
 // is a seed, 30's second chunk would need 31's values; the other half of the
 // CTA covers those blocks).
-template <int L1>
+template <int L1, int GS>
 __device__ __forceinline__ void put_exchange_t(float *xs, int b, bool wr, const float (&t2)[8][8]) {
 #pragma unroll
   for (int h = 0; h < 8; ++h) {
     constexpr int dummy = 0;
     (void)dummy;
-    const int sh = L1 * h, qh = sh >> 2, mh = sh & 3;
+    const int sh = L1 * (h & ((1 << GS) - 1)), qh = sh >> 2, mh = sh & 3;
     float nx[4];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -177,13 +232,13 @@ __device__ __forceinline__ int g2_block() {
   return (threadIdx.x >> 7) ? 30 + lane : lane;
 }
 
-template <int L1>
+template <int L1, int GS = 3>
 __device__ __forceinline__ void group2t_and_exchange(float (&a)[8][8], float *xs, bool edge, int kc, int ap) {
   float t2[8][8];
   const int b = g2_block();
-  group2t<L1>(a, t2, edge, kc, ap, 8 * b);
+  group2t<L1, GS>(a, t2, edge, kc, ap, 8 * b);
   const int lane = threadIdx.x & 31;
-  put_exchange_t<L1>(xs, b, lane < 30, t2);
+  put_exchange_t<L1, GS>(xs, b, lane < 30, t2);
 }
 
 // Group 1t for one sweep: chunk ch of combo h's four angle rows -> members
@@ -240,12 +295,14 @@ __device__ __forceinline__ void group1t(const float *xs, int h, int ch, float (&
   }
 }
 
-// ---- pass 1 (forward stages 5..9 undone, n = 1024) ------------------------
+// ---- pass 1 (the last five forward stages undone, L-1 .. L-5) --------------
 // Input: the (4, 2n-1, n) array, angles 32 a' .. 32 a' + 31 (128 bytes per
-// offset); output: bdrt buffer rows (a', member i) at reference offset
-// u - a' i, row stride cs.  A4 = a' mod 4 fixes each member's sub-chunk shift.
-template <int A4>
+// offset), a' < n / 32; output: bdrt buffer rows (a', member i) = level L-5
+// angle a', section i, at reference offset u - a' i, row stride cs.
+// A4 = a' mod 4 fixes each member's sub-chunk shift.
+template <int A4, int NN>
 __device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *rows_ap, int ap, int c0, int h) {
+  using G = Geo<NN>;
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
@@ -254,7 +311,7 @@ __device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *ro
     constexpr int dummy = 0;
     (void)dummy;
     const int mi = (A4 * m) & 3;  // == D & 3
-    float *row = rows_ap + i * CS1;
+    float *row = rows_ap + i * G::cs;
     // Chunk X = ch + c0/4 - D/4 of the member's row; stored when it holds
     // stored tile positions and lies in [0, 2n-1): X in [0, ceil(C/4)).
     const int X0 = lane + (c0 >> 2) - (D >> 2);
@@ -276,16 +333,18 @@ __device__ __forceinline__ void pass1_store(const float (&o)[4][4][4], float *ro
       const int X = X0 + 31 * it;
       // lane < 31 and 4 ch + mi < W, ch = 31 it + lane
       const int lane_lim = min(31, (W - mi + 3) / 4 - 31 * it);
-      if (lane < lane_lim && (unsigned)X < (unsigned)((C1 + 3) / 4))
+      if (lane < lane_lim && (unsigned)X < (unsigned)((G::C + 3) / 4))
         *reinterpret_cast<float4 *>(row + 4 * X) = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 }
 
+template <int NN>
 __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ in, float *__restrict__ buf,
                                                       int need) {
+  using G = Geo<NN>;
   extern __shared__ __align__(16) float xs[];
-  constexpr int n = N1, C = C1;
+  constexpr int n = G::n, C = G::C;
   const int c0 = (int)blockIdx.x * W;
   const int bq = (int)blockIdx.y;  // image * 4 + quadrant
   const int ap = (int)blockIdx.z;
@@ -337,41 +396,46 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
   float o[4][4][4];
 #pragma unroll
   for (int it = 0; it < 4; ++it) group1t(xs, h, 31 * it + (threadIdx.x & 31), o[it], edge, kc, ap);
-  float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * CS1;
+  float *rows_ap = buf + ((size_t)bq * n + (size_t)ap * 32) * G::cs;
   switch (ap & 3) {
-    case 0: pass1_store<0>(o, rows_ap, ap, c0, h); break;
-    case 1: pass1_store<1>(o, rows_ap, ap, c0, h); break;
-    case 2: pass1_store<2>(o, rows_ap, ap, c0, h); break;
-    default: pass1_store<3>(o, rows_ap, ap, c0, h); break;
+    case 0: pass1_store<0, NN>(o, rows_ap, ap, c0, h); break;
+    case 1: pass1_store<1, NN>(o, rows_ap, ap, c0, h); break;
+    case 2: pass1_store<2, NN>(o, rows_ap, ap, c0, h); break;
+    default: pass1_store<3, NN>(o, rows_ap, ap, c0, h); break;
   }
 }
 
-// ---- pass 2 (forward stages 0..4 undone, any n >= 256) ---------------------
-// Input: bdrt buffer rows (angle l, section r) for l < 32, row stride cs;
-// output: (4, 2n-1, n) sections 32 r .. 32 r + 31 (128 bytes per offset),
-// staged in shared memory (chunk h of row p at chunk h ^ ((p >> 2) & 7)).
+// ---- pass 2 (the first S = L-5 forward stages undone, S-1 .. 0) ----------
+// Input: bdrt buffer rows of level S (2^S angles x 32 sections, row angle *
+// 32 + section, row stride cs); a CTA takes the 32 rows of sections
+// (32 >> S) R .. (32 >> S) R + (32 >> S) - 1, all angles; output: (4, 2n-1, n)
+// sections 32 R .. 32 R + 31 (128 bytes per offset), staged in shared memory
+// (chunk h of row p at chunk h ^ ((p >> 2) & 7)).
 template <int NN>
 __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ buf, float *__restrict__ out,
                                                       int need) {
+  using G = Geo<NN>;
   extern __shared__ __align__(16) float xs[];
-  constexpr int n = NN, C = 2 * n - 1, cs = (C + 7) / 8 * 8;
+  constexpr int n = G::n, C = G::C, cs = G::cs, S = G::S, GS = G::GS;
   const int c0 = (int)blockIdx.x * W;
   if (c0 >= need) return;
   const int bq = (int)blockIdx.y;
   const int r = (int)blockIdx.z;
-  const int R = n / 32;  // sections per angle row group
   const int L1 = (threadIdx.x >> 5) & 3, b = g2_block();
   const int kc = C - c0;
   const bool edge = kc < TWI;
   const int e0 = 8 * b;  // lane's first tile position
-  const float *src = buf + (size_t)bq * n * cs + ((size_t)(8 * L1) * R + r) * cs + c0 + e0;
+  const float *src = buf + (size_t)bq * n * cs + c0 + e0;
+  // Row l3 of this lane: set l3 >> GS (section (32 >> S) r + that), angle
+  // 2^GS L1 + (l3 mod 2^GS); at n = 1024 angle 8 L1 + l3 of section r.
   // Chunks that start at or past 2n-1 read +0 without a memory access (the
   // last chunk of a row ends exactly at 2n-1); offset 2n-1 itself is set
   // below: -0 on the odd angles (B rows), +0 on the even ones.
   float a[8][8];
 #pragma unroll
   for (int l3 = 0; l3 < 8; ++l3) {
-    const float *p = src + (size_t)l3 * R * cs;
+    const int angle = (L1 << GS) + (l3 & ((1 << GS) - 1)), section = (32 >> S) * r + (l3 >> GS);
+    const float *p = src + (size_t)(angle * 32 + section) * cs;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v0 = ld4_cs_if(p, e0 < kc, zero), v1 = ld4_cs_if(p + 4, e0 + 4 < kc, zero);
     a[l3][0] = v0.x; a[l3][1] = v0.y; a[l3][2] = v0.z; a[l3][3] = v0.w;
@@ -382,13 +446,13 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
     for (int l3 = 0; l3 < 8; ++l3)
 #pragma unroll
       for (int k = 0; k < 8; ++k)
-        if (e0 + k == kc) a[l3][k] = (l3 & 1) ? -0.f : 0.f;
+        if (e0 + k == kc) a[l3][k] = ((GS > 0 ? l3 : L1) & 1) ? -0.f : 0.f;
   }
   switch (L1) {
-    case 0: group2t_and_exchange<0>(a, xs, edge, kc, 0); break;
-    case 1: group2t_and_exchange<1>(a, xs, edge, kc, 0); break;
-    case 2: group2t_and_exchange<2>(a, xs, edge, kc, 0); break;
-    default: group2t_and_exchange<3>(a, xs, edge, kc, 0); break;
+    case 0: group2t_and_exchange<0, GS>(a, xs, edge, kc, 0); break;
+    case 1: group2t_and_exchange<1, GS>(a, xs, edge, kc, 0); break;
+    case 2: group2t_and_exchange<2, GS>(a, xs, edge, kc, 0); break;
+    default: group2t_and_exchange<3, GS>(a, xs, edge, kc, 0); break;
   }
   __syncthreads();
   const int h = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -426,24 +490,25 @@ __global__ void __launch_bounds__(NT, 2) pass2_kernel(const float *__restrict__ 
 }  // namespace bfast
 
 // Column tiles: pass 2 covers offsets [0, 2n-1); pass 1 tile positions
-// [0, 2n-1 + 31 * 31) (member i of input angle group a' is stored 31 a'
-// positions to the left at most).
+// [0, 2n-1 + 31 (n/32 - 1)) (member i of input angle group a' is stored
+// a' i positions to the left).
 static int pass_tiles(i64 n, bool first) {
-  const i64 span = 2 * n - 1 + (first ? 31 * 31 : 0);
+  const i64 span = 2 * n - 1 + (first ? 31 * (n / 32 - 1) : 0);
   return (int)((span + bfast::W - 1) / bfast::W);
 }
 
-int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+template <int NN>
+static int launch_pass1(const float *in, float *buf, i64 batch, i64 need, cudaStream_t st) {
+  using G = bfast::Geo<NN>;
   static std::atomic<unsigned long long> configured{0};
-  if (const int rc = smem_limit_once((const void *)bfast::pass1_kernel, bfast::SMEM, configured)) return rc;
-  const int tiles = pass_tiles(n, true);
-  if (n != bfast::N1 || cs != bfast::CS1) return ADRT_GB300_ERR_SHAPE;
+  if (const int rc = smem_limit_once((const void *)bfast::pass1_kernel<NN>, bfast::SMEM, configured)) return rc;
+  const int tiles = pass_tiles(NN, true);
   // Grid y counts (image, quadrant) pairs: launches of at most 16383 images.
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
-    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), 32);
-    bfast::pass1_kernel<<<grid, bfast::NT, bfast::SMEM, st>>>(in + b0 * 4 * (2 * n - 1) * n, buf + b0 * 4 * n * cs,
-                                                                (int)need);
+    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(NN / 32));
+    bfast::pass1_kernel<NN><<<grid, bfast::NT, bfast::SMEM, st>>>(in + b0 * 4 * G::C * NN,
+                                                                    buf + b0 * 4 * NN * G::cs, (int)need);
     if (const int rc = launch_status()) return rc;
   }
   return ADRT_GB300_OK;
@@ -451,24 +516,36 @@ int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 n
 
 template <int NN>
 static int launch_pass2(const float *buf, float *out, i64 batch, i64 need, cudaStream_t st) {
-  constexpr i64 n = NN, cs = (2 * NN - 1 + 7) / 8 * 8;
+  using G = bfast::Geo<NN>;
   static std::atomic<unsigned long long> configured{0};
   if (const int rc = smem_limit_once((const void *)bfast::pass2_kernel<NN>, bfast::SMEM, configured)) return rc;
-  const int tiles = pass_tiles(n, false);
+  const int tiles = pass_tiles(NN, false);
   for (i64 b0 = 0; b0 < batch; b0 += 16383) {
     const i64 nb = batch - b0 < 16383 ? batch - b0 : 16383;
-    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(n / 32));
-    bfast::pass2_kernel<NN><<<grid, bfast::NT, bfast::SMEM, st>>>(buf + b0 * 4 * n * cs,
-                                                                    out + b0 * 4 * (2 * n - 1) * n, (int)need);
+    const dim3 grid((unsigned)tiles, (unsigned)(nb * 4), (unsigned)(NN / 32));
+    bfast::pass2_kernel<NN><<<grid, bfast::NT, bfast::SMEM, st>>>(buf + b0 * 4 * NN * G::cs,
+                                                                    out + b0 * 4 * G::C * NN, (int)need);
     if (const int rc = launch_status()) return rc;
   }
   return ADRT_GB300_OK;
 }
 
 // The bdrt buffer's rows are padded to 8 floats (cs = (2n - 1 + 7) / 8 * 8).
+int bdrt_fast_pass1(const float *in, float *buf, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
+  if (cs != (2 * n - 1 + 7) / 8 * 8) return ADRT_GB300_ERR_SHAPE;
+  switch (n) {
+    case 128: return launch_pass1<128>(in, buf, batch, need, st);
+    case 256: return launch_pass1<256>(in, buf, batch, need, st);
+    case 512: return launch_pass1<512>(in, buf, batch, need, st);
+    case 1024: return launch_pass1<1024>(in, buf, batch, need, st);
+  }
+  return ADRT_GB300_ERR_SHAPE;
+}
+
 int bdrt_fast_pass2(const float *buf, float *out, i64 batch, i64 n, i64 cs, i64 need, cudaStream_t st) {
   if (cs != (2 * n - 1 + 7) / 8 * 8) return ADRT_GB300_ERR_SHAPE;
   switch (n) {
+    case 128: return launch_pass2<128>(buf, out, batch, need, st);
     case 256: return launch_pass2<256>(buf, out, batch, need, st);
     case 512: return launch_pass2<512>(buf, out, batch, need, st);
     case 1024: return launch_pass2<1024>(buf, out, batch, need, st);

@@ -1,5 +1,6 @@
-"""The register-level bdrt passes (float32, 256 <= n <= 1024) against the
-oracle, bit for bit: signed zeros, infinities and NaNs spread over whole rows,
+"""The register-level bdrt passes (float32, 128 <= n <= 1024: the last five
+forward stages undone by the first pass, the first L-5 by the second) against
+the oracle, bit for bit: signed zeros, infinities and NaNs spread over whole rows,
 dense near the row ends (where the reference's copy and zero rules act, in the
 tiles the generic kernel keeps) and around the offsets where the register
 tiles end; the truncated bdrt of the adjoint; batches large enough to need
@@ -37,7 +38,7 @@ def _hard_input(rng, b, n, dtype=np.float32):
     return y
 
 
-@pytest.mark.parametrize("n,b", [(256, 3), (512, 2), (1024, 2)])
+@pytest.mark.parametrize("n,b", [(128, 5), (256, 3), (512, 2), (1024, 2)])
 def test_bdrt_fast_bit_exact(oracle_mod, n, b):
     rng = np.random.default_rng(n)
     y = _hard_input(rng, b, n)
@@ -46,7 +47,7 @@ def test_bdrt_fast_bit_exact(oracle_mod, n, b):
     assert bits_equal(got, want), first_mismatch(got, want)
 
 
-@pytest.mark.parametrize("n", [256, 1024])
+@pytest.mark.parametrize("n", [128, 256, 512, 1024])
 def test_adjoint_fast_bit_exact(oracle_mod, n):
     rng = np.random.default_rng(n + 1)
     y = rng.standard_normal((2, 4, 2 * n - 1, n)).astype(np.float32)
@@ -56,9 +57,9 @@ def test_adjoint_fast_bit_exact(oracle_mod, n):
     assert bits_equal(got, want), first_mismatch(got, want)
 
 
-def test_bdrt_fast_many_images(oracle_mod):
-    # 40 images at n = 256: one chunk, one launch per pass; every image checked.
-    n, b = 256, 40
+@pytest.mark.parametrize("n,b", [(256, 40), (512, 12), (128, 64)])
+def test_bdrt_fast_many_images(oracle_mod, n, b):
+    # Many images: one chunk, one launch per pass; every image checked.
     g = torch.Generator(device="cuda")
     g.manual_seed(7)
     y = torch.randn((b, 4, 2 * n - 1, n), generator=g, device="cuda")
