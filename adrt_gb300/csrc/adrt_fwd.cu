@@ -312,11 +312,6 @@ int fast_inter_cs(i64 n);
 int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, size_t ws_bytes,
                       cudaStream_t st);
 
-int fwd_first_pass_padded(const float *in, float *inter, i64 batch, i64 n, int stages, int cs,
-                          cudaStream_t st) {
-  FwdPassArgs a{in, inter, n, 0, batch, cs};
-  return dispatch_pass<float>(stages, true, false, a, st);
-}
 
 static bool use_fast_path(i64 n, size_t elem) {
   return fast_forward_eligible(n, elem) && tune_lookup(ADRT_GB300_OP_ADRT, ADRT_GB300_F32, n).use_fast != 0;
@@ -391,7 +386,7 @@ template int adrt_forward<double>(const double *, double *, i64, i64, void *, si
 
 // Item kinds: a generic pass tile, or a tile of the fast float32 passes
 // (pass A at n = 1024; pass B for 64 <= n <= 1024, reading the padded
-// intermediate [q][32][n/32][cs] that pass A or a generic first pass wrote).
+// intermediate [q][32][n/32][cs] that pass A wrote).
 enum { RAGGED_GENERIC = 0, RAGGED_FAST_A = 1, RAGGED_FAST_B = 2 };
 
 struct RaggedImage {
@@ -459,7 +454,8 @@ __device__ __forceinline__ void ragged_fast_a_item(int S, const float *img, floa
     case 5: ragged_fast_a_tile<5>(img, inter_img, t, xs, hook); break;
     case 4: ragged_fast_a_tile<4>(img, inter_img, t, xs, hook); break;
     case 3: ragged_fast_a_tile<3>(img, inter_img, t, xs, hook); break;
-    default: ragged_fast_a_tile<2>(img, inter_img, t, xs, hook); break;
+    case 2: ragged_fast_a_tile<2>(img, inter_img, t, xs, hook); break;
+    default: ragged_fast_a_tile<1>(img, inter_img, t, xs, hook); break;
   }
 }
 
@@ -649,11 +645,10 @@ static RaggedImagePlan ragged_image_plan(i64 n, size_t elem, bool fast) {
     ip.s0 = L - 5;
     ip.s1 = 5;
     ip.cs = fast_inter_cs(n);
-    // n >= 128: the register first pass (S = L - 5 >= 2 stages); n = 64:
-    // the generic one.
-    ip.kind0 = n >= 128 ? RAGGED_FAST_A : RAGGED_GENERIC;
+    // The register first pass (S = L - 5 >= 1 stages).
+    ip.kind0 = RAGGED_FAST_A;
     ip.kind1 = RAGGED_FAST_B;
-    ip.tiles0 = n >= 128 ? 4 * (n / 32) * ((ip.cs + fast::W - 1) / fast::W) : fwd_pass_tiles(n, ip.s0, kFwdWNarrow);
+    ip.tiles0 = 4 * (n / 32) * ((ip.cs + fast::W - 1) / fast::W);
     ip.tiles1 = 4 * (n / 32) * fast::pass_b_col_tiles((int)n);
     ip.inter_elems = 4 * n * ip.cs;
     return ip;

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(NT, 2) pass_b_kernel(const float *__restrict__
 static int fast_cs(i64 n) { return (int)((n + n / 32 - 1 + 7) / 8 * 8); }
 static_assert(fast::CS == (fast::N + fast::N / 32 - 1 + 7) / 8 * 8, "row stride at n = 1024");
 static_assert(fast::PassA<5>::CS == fast::CS && fast::PassA<4>::CS == 528 && fast::PassA<3>::CS == 264 &&
-                  fast::PassA<2>::CS == 136,
+                  fast::PassA<2>::CS == 136 && fast::PassA<1>::CS == 72,
               "pass A row strides equal the intermediate's");
 
 int fast_inter_cs(i64 n) { return fast_cs(n); }
@@ -94,11 +94,6 @@ static i64 fast_chunk(i64 batch, i64 n) {
 }
 
 size_t fast_workspace_bytes(i64 batch, i64 n) { return fast_inter_bytes(n) * (size_t)fast_chunk(batch, n); }
-
-// First pass for n < 1024: the generic kernel runs stages 0..L-6 and writes
-// the padded intermediate (adrt_fwd.cu).
-int fwd_first_pass_padded(const float *in, float *inter, i64 batch, i64 n, int stages, int cs,
-                          cudaStream_t st);
 
 // Device-side error word of the fast kernels (raised when a bounded wait for
 // bulk copies expires); read and cleared by adrt_gb300_device_status.
@@ -135,18 +130,14 @@ int adrt_forward_fast(const float *in, float *out, i64 batch, i64 n, void *ws, s
   for (i64 b0 = 0; b0 < batch; b0 += chunk) {
     const int nb = (int)((batch - b0) < chunk ? (batch - b0) : chunk);
     int rc;
-    // First L-5 stages: the register pass for n >= 128, the generic pass at
-    // n = 64 (one stage).
+    // First L-5 stages: the register pass.
     const float *src = in + b0 * n * n;
-    if (n >= 128) {
-      switch (L) {
-        case 10: rc = fast::launch_pass_a<5>(src, inter, nb, st); break;
-        case 9: rc = fast::launch_pass_a<4>(src, inter, nb, st); break;
-        case 8: rc = fast::launch_pass_a<3>(src, inter, nb, st); break;
-        default: rc = fast::launch_pass_a<2>(src, inter, nb, st); break;
-      }
-    } else {
-      rc = fwd_first_pass_padded(src, inter, nb, n, L - 5, cs, st);
+    switch (L) {
+      case 10: rc = fast::launch_pass_a<5>(src, inter, nb, st); break;
+      case 9: rc = fast::launch_pass_a<4>(src, inter, nb, st); break;
+      case 8: rc = fast::launch_pass_a<3>(src, inter, nb, st); break;
+      case 7: rc = fast::launch_pass_a<2>(src, inter, nb, st); break;
+      default: rc = fast::launch_pass_a<1>(src, inter, nb, st); break;
     }
     if (rc) return rc;
     const dim3 gridb((unsigned)(col_tiles * 4), (unsigned)nb, (unsigned)(n / 32));

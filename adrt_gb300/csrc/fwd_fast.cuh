@@ -55,11 +55,12 @@ constexpr unsigned FULL = 0xffffffffu;
 // offsets below n + 2^S - 1, rounded up to 8 floats.
 template <int S>
 struct PassA {
-  static_assert(S >= 2 && S <= 5, "pass A runs 2 to 5 stages");
+  static_assert(S >= 1 && S <= 5, "pass A runs 1 to 5 stages");
   static constexpr int n = 32 << S;
-  static constexpr int CS = (n + n / 32 - 1 + 7) / 8 * 8;  // 1056, 528, 264, 136
-  static constexpr int TILES = (CS + W - 1) / W;            // 3, 2, 1, 1
-  static constexpr int GS = S - 2;                          // stages of group 2
+  static constexpr int CS = (n + n / 32 - 1 + 7) / 8 * 8;  // 1056, 528, 264, 136, 72
+  static constexpr int TILES = (CS + W - 1) / W;            // 3, 2, 1, 1, 1
+  static constexpr int GS = S >= 2 ? S - 2 : 0;             // stages of group 2
+  static constexpr int G1 = S >= 2 ? 2 : 1;                 // stages of group 1
 };
 
 // Sweep iterations pass A's column tile ct needs for n = 32 * 2^S (the
@@ -126,7 +127,9 @@ struct G1Tail {
   float s10, s11a, s11b; // stage-0 odd-pair outputs: li=0 pos 3, li=1 pos 3, li=1 pos 2
 };
 
-template <int D>
+// ST = 1 (pass A at n = 64, one stage): stage 0 only, o[2 pair + p] =
+// pair (0,1) or (2,3) at angle p.
+template <int D, int ST = 2>
 __device__ __forceinline__ void group1_compute(const float (&m)[4][4], float (&o)[4][4],
                                                G1Tail &saved, int lane) {
   // stage 0: pairs (0,1) and (2,3); shift p for the odd member.
@@ -145,33 +148,40 @@ __device__ __forceinline__ void group1_compute(const float (&m)[4][4], float (&o
     s0[0][1][k] = add_rn(m[0][k], k ? m[1][k - 1] : pm1);
     s0[1][1][k] = add_rn(m[2][k], k ? m[3][k - 1] : pm3);
   }
-  // stage 1: combo 0 (pair 0) + combo 1 (pair 1) shifted by li + p.
-  const float q0 = prev_chunk<D>(s0[1][0][3], saved.s10, lane);   // li=0, position -1
-  const float q1 = prev_chunk<D>(s0[1][1][3], saved.s11a, lane);  // li=1, position -1
-  const float q2 = prev_chunk<D>(s0[1][1][2], saved.s11b, lane);  // li=1, position -2
-  saved.s10 = s0[1][0][3];
-  saved.s11a = s0[1][1][3];
-  saved.s11b = s0[1][1][2];
-  // ext[li][k + 2] = odd combo value at position k (k in [-2, 4))
-  float ext0[6], ext1[6];
-  ext0[0] = 0.f;  // never used (shift <= 1 for li = 0)
-  ext0[1] = q0;
-  ext1[0] = q2;
-  ext1[1] = q1;
+  if constexpr (ST == 1) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    ext0[k + 2] = s0[1][0][k];
-    ext1[k + 2] = s0[1][1][k];
-  }
+    for (int l = 0; l < 4; ++l)
 #pragma unroll
-  for (int k = 0; k < 4; k += 2) {
-    add_rn2(s0[0][0][k], s0[0][0][k + 1], ext0[k + 2], ext0[k + 3], o[0][k], o[0][k + 1]);  // li=0, p=0
-    add_rn2(s0[0][1][k], s0[0][1][k + 1], ext1[k], ext1[k + 1], o[3][k], o[3][k + 1]);      // li=1, p=1
-  }
+      for (int k = 0; k < 4; ++k) o[l][k] = s0[l >> 1][l & 1][k];
+  } else {
+    // stage 1: combo 0 (pair 0) + combo 1 (pair 1) shifted by li + p.
+    const float q0 = prev_chunk<D>(s0[1][0][3], saved.s10, lane);   // li=0, position -1
+    const float q1 = prev_chunk<D>(s0[1][1][3], saved.s11a, lane);  // li=1, position -1
+    const float q2 = prev_chunk<D>(s0[1][1][2], saved.s11b, lane);  // li=1, position -2
+    saved.s10 = s0[1][0][3];
+    saved.s11a = s0[1][1][3];
+    saved.s11b = s0[1][1][2];
+    // ext[li][k + 2] = odd combo value at position k (k in [-2, 4))
+    float ext0[6], ext1[6];
+    ext0[0] = 0.f;  // never used (shift <= 1 for li = 0)
+    ext0[1] = q0;
+    ext1[0] = q2;
+    ext1[1] = q1;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    o[1][k] = add_rn(s0[0][0][k], ext0[k + 1]);      // li=0, p=1
-    o[2][k] = add_rn(s0[0][1][k], ext1[k + 1]);      // li=1, p=0
+    for (int k = 0; k < 4; ++k) {
+      ext0[k + 2] = s0[1][0][k];
+      ext1[k + 2] = s0[1][1][k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k += 2) {
+      add_rn2(s0[0][0][k], s0[0][0][k + 1], ext0[k + 2], ext0[k + 3], o[0][k], o[0][k + 1]);  // li=0, p=0
+      add_rn2(s0[0][1][k], s0[0][1][k + 1], ext1[k], ext1[k + 1], o[3][k], o[3][k + 1]);      // li=1, p=1
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      o[1][k] = add_rn(s0[0][0][k], ext0[k + 1]);      // li=0, p=1
+      o[2][k] = add_rn(s0[0][1][k], ext1[k + 1]);      // li=1, p=0
+    }
   }
 }
 
@@ -249,7 +259,7 @@ __device__ __forceinline__ void group1_passA_rows(const float *img, int q, int r
       m[jj][2] = raw[it][jj].y; m[jj][3] = raw[it][jj].x;
     }
     float o[4][4];
-    group1_compute<1>(m, o, saved, lane);
+    group1_compute<1, NI == 64 ? 1 : 2>(m, o, saved, lane);
     put_exchange(xs, mq, it * 32 + lane, o);
   }
 }
@@ -293,7 +303,7 @@ __device__ __forceinline__ void group1_passA_cols(const float *img, int q, int r
       m[2][k] = raw[it][k].z; m[3][k] = raw[it][k].w;
     }
     float o[4][4];
-    group1_compute<8>(m, o, saved, lane);
+    group1_compute<8, NI == 64 ? 1 : 2>(m, o, saved, lane);
     if (live && ch >= 16 * w) put_exchange(xs, mq, ch, o);
   }
 }
@@ -522,6 +532,8 @@ __device__ __forceinline__ int first_stored_block() { return (threadIdx.x >> 7) 
 // Pass A's group 2 for S stages: stores the 8 rows of this lane's block.
 // Row e of `out` is row group (32 >> S) R + (e >> GS) at angle 2^GS L1 +
 // (e mod 2^GS); inter_q = the quadrant's intermediate [g (32)][a (2^S)][CS].
+// S = 1: group 1 did the only stage and its angle l1 = 2 pair + p, so row e
+// (quad h = e) is row group 16 R + 2 e + (L1 >> 1) at angle L1 & 1.
 template <int L1, int S>
 __device__ __forceinline__ void group2_passA(const float *xs, float *inter_q, int R, int c0) {
   using P = PassA<S>;
@@ -535,8 +547,8 @@ __device__ __forceinline__ void group2_passA(const float *xs, float *inter_q, in
   if (store && d0 < P::CS) {
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-      const int g = (R << (3 - P::GS)) + (e >> P::GS);
-      const int a = (L1 << P::GS) + (e & ((1 << P::GS) - 1));
+      const int g = S == 1 ? 16 * R + 2 * e + (L1 >> 1) : (R << (3 - P::GS)) + (e >> P::GS);
+      const int a = S == 1 ? L1 & 1 : (L1 << P::GS) + (e & ((1 << P::GS) - 1));
       st8(inter_q + ((size_t)g * (1 << S) + a) * P::CS + d0, out[e]);
     }
   }

@@ -1,4 +1,4 @@
-"""The register-level first pass of the float32 forward at n = 128, 256, 512
+"""The register-level first pass of the float32 forward at n = 64 .. 512
 (the first log2(n) - 5 stages, then the five-stage second pass) against the
 oracle, bit for bit: signed zeros along whole rows and columns (the four
 quadrants read rows from the right end and columns up and down), infinities
@@ -30,7 +30,7 @@ def _hard_image(rng, b, n):
     return x
 
 
-@pytest.mark.parametrize("n,b", [(128, 5), (256, 3), (512, 2)])
+@pytest.mark.parametrize("n,b", [(64, 7), (128, 5), (256, 3), (512, 2)])
 def test_first_pass_bit_exact(oracle_mod, n, b):
     rng = np.random.default_rng(n + 17)
     x = _hard_image(rng, b, n)
@@ -39,7 +39,7 @@ def test_first_pass_bit_exact(oracle_mod, n, b):
     assert bits_equal(got, want), first_mismatch(got, want)
 
 
-@pytest.mark.parametrize("n", [128, 256, 512])
+@pytest.mark.parametrize("n", [64, 128, 256, 512])
 def test_first_pass_many_images(oracle_mod, n):
     # Enough images for several CTAs per SM at every size; all checked.
     b = 64 if n < 512 else 24
