@@ -1,6 +1,7 @@
-// Device code of the fast forward ADRT for float32 (two passes of five stages):
-// the per-tile functions the standalone pass kernels (adrt_fwd_fast.cu) and
-// the ragged persistent kernel (adrt_fwd.cu) run.
+// Device code of the fast forward ADRT for float32, n = 64..1024, in two
+// passes: pass A the first S = log2(n) - 5 stages (1 to 5), pass B the last
+// five.  The per-tile functions the standalone pass kernels
+// (adrt_fwd_fast.cu) and the ragged persistent kernel (adrt_fwd.cu) run.
 //
 // Same decomposition as adrt_fwd.cu: a pass merges 32 members (rows in pass A,
 // row groups in pass B) at input angle a' into 32 angles, member i loaded with
@@ -8,7 +9,8 @@
 // This kernel keeps those five stages out of shared memory as much as the
 // hardware allows:
 //
-//  group 1 (stages 0-1): each lane owns 4 members x 4 consecutive positions
+//  group 1 (stages 0-1; stage 0 only in a one-stage pass A): each lane owns
+//    4 members x 4 consecutive positions
 //    (one 16-byte chunk per member, loaded straight from global memory with
 //    128-bit loads).  A warp sweeps the tile in iterations of 32 chunks; the
 //    few operands that cross a chunk boundary come from the neighbouring lane
@@ -18,6 +20,7 @@
 //  group 2 (stages 2-4): each lane owns 8 combos x 8 positions of one angle
 //    l1 of group 1.  Combo h is read pre-shifted by l1*h, which leaves a fresh
 //    3-stage butterfly with shifts <= 4; boundary operands come from lane-1.
+//    A pass A of S < 5 stages runs S - 2 of them on sets of combos.
 //
 // Operands whose reference offset is negative are "absent" (the reference
 // copies instead of adding).  They are loaded as -0.0f, and e + (-0) == e bit
@@ -656,8 +659,9 @@ __device__ __forceinline__ void pass_a_tile(const float *img, float *inter_img, 
 // One pass-B tile (any n in [64, 1024]): quadrant q, input angle a' = ap,
 // column tile ct of one image; inter_img = its intermediate [q][g (32)]
 // [a (n/32)][cs], out_img = its (4, 2n-1, n) output.  LD: cache mode of the
-// intermediate's loads; FULL_SWEEP as for pass_a_tile (the live rows are
-// stored either way).
+// intermediate's loads.  FULL_SWEEP: every tile sweeps all positions (a
+// persistent loop around a sweep of run-time length spills); the live rows
+// are stored either way.
 template <int LD, bool FULL_SWEEP = false, class Hook = NoHook>
 __device__ __forceinline__ void pass_b_tile(const float *inter_img, float *out_img, int n, int cs, int q, int ap,
                                             int ct, float *xs, const Hook &hook = Hook()) {
