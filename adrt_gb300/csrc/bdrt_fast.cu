@@ -1,5 +1,6 @@
-// Register-level bdrt passes for float32 (the transpose of the fast forward's
-// five-stage pass structure).
+// Register-level bdrt passes for float32, n = 128..1024 (the transpose of the
+// fast forward's pass structure): pass 1 undoes the last five forward stages,
+// pass 2 the first S = log2(n) - 5.
 //
 // The generic pass (bdrt.cu) holds a tile of 32 rows in shared memory and
 // runs each transposed stage through it.  Here a pass's five stages run in
@@ -20,11 +21,12 @@
 // Row (combo m, level J) sits at tile position u <-> reference offset
 // c0 + u - a' m 2^J; in group 2t's frame (below) also + L1 m 2^(J-2).
 //
-//  group 2t (stages 4, 3, 2 undone): a lane holds the 8 angles 8 L1 + l3 at 8
-//    consecutive positions (block b); operands to the right come from lane+1
-//    by shuffle.  The L1-dependent part of the shifts (4 L1, 2 L1, L1) is left
-//    out, so level-2 combo h comes out L1 * h positions to the right of its
-//    tile position; the exchange write puts it back.
+//  group 2t (stages 4, 3, 2 undone; in a pass 2 of S < 5 stages, S - 2 of
+//    them on per-section sets of rows): a lane holds the 8 angles 8 L1 + l3
+//    at 8 consecutive positions (block b); operands to the right come from
+//    lane+1 by shuffle.  The L1-dependent part of the shifts (4 L1, 2 L1, L1)
+//    is left out, so level-2 combo h comes out L1 * h positions to the right
+//    of its tile position; the exchange write puts it back.
 //  exchange: level-2 rows (combo h, angle L1) in shared memory, 16-byte chunks
 //    XOR-swizzled as in the forward kernel.
 //  group 1t (stages 1, 0 undone): a warp owns combo h, a lane one 4-position
