@@ -784,6 +784,8 @@ def main():
             "h2d_bytes_per_step": int(xh.numel() * xh.element_size()),
             "d2h_bytes_per_step": int(yh.numel() * yh.element_size()),
             "windows_img_s": [world * B * args.e2e_steps / w for w in windows],
+            # The median call, a figure that single slow calls do not move.
+            "median_call_img_s": world * B / (statistics.median(call_ms) / 1e3),
             "window": f"best of 5 windows of {args.e2e_steps} calls",
             "warmup_call_ms": warm_ms,
             "call_ms": call_ms,
