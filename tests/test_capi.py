@@ -106,5 +106,10 @@ def test_workspace_sizes(lib):
     got64 = _lib.workspace_size(_lib.OP_ADRT, 8, 512, _lib.F64)
     assert got64 > 0 and got64 % per64 == 0
     assert _lib.workspace_size(_lib.OP_IADRT, 2, 64, _lib.F64) == 2 * 2 * 4 * 64 * 127 * 8
+    # bdrt: one buffer between its two passes; on the float32 register path
+    # (128 <= n <= 1024) its rows are padded from 2n - 1 to 2n floats.
+    for n in (128, 256, 512, 1024):
+        assert _lib.workspace_size(_lib.OP_BDRT, 3, n, _lib.F32) == 3 * 4 * n * (2 * n) * 4
+    assert _lib.workspace_size(_lib.OP_BDRT, 3, 64, _lib.F32) == 3 * 4 * 64 * 127 * 4
     with pytest.raises(ValueError):
         _lib.workspace_size(_lib.OP_ADRT, 1, 12, _lib.F32)
