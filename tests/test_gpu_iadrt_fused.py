@@ -52,3 +52,22 @@ def test_iadrt_fused_many_images(oracle_mod):
         assert torch.equal(inv[i], adrt.iadrt(y[i]))
         want = oracle_mod.iadrt(y[i].cpu().numpy())
         assert bits_equal(inv[i].cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("n,b,dt", [(64, 640, np.float32), (256, 160, np.float32), (128, 320, np.float64)])
+def test_iadrt_row_sweep_bit_exact(oracle_mod, n, b, dt):
+    # Batches with at least 32 warps of chains per SM (4 b n >= 152 x 1024)
+    # take the single-stage kernels' row sweep for the odd chains; each
+    # image must equal its own (per-lane sweep) call and the oracle.
+    assert 4 * b * n >= 152 * 1024
+    rng = np.random.default_rng(n + b)
+    y = _hard(rng, b, n, dt)
+    yd = torch.from_numpy(y).cuda()
+    got = adrt.iadrt(yd)
+    g = got.cpu().numpy()
+    for i in (0, 1, b // 2, b - 1):  # bit patterns: the last image holds a NaN
+        one = adrt.iadrt(yd[i]).cpu().numpy()
+        assert bits_equal(g[i], one), (i, first_mismatch(g[i], one))
+    for i in (0, b - 1):
+        want = oracle_mod.iadrt(y[i])
+        assert bits_equal(g[i], want), first_mismatch(g[i], want)
