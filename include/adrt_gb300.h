@@ -126,7 +126,11 @@ int adrt_gb300_adrt_noalloc(const void *in, void *out, int64_t batch, int64_t n,
  * CTAs take (image, pass, tile) items from a device-side queue; second-pass
  * items wait, with a bounded device-side wait, for their image's first pass.
  * After the call, adrt_gb300_ragged_status synchronises the stream and
- * reports ADRT_GB300_ERR_TIMEOUT if any wait expired. */
+ * reports ADRT_GB300_ERR_TIMEOUT if any wait expired.  The call does not
+ * wait for the GPU: its descriptors are uploaded from a pinned staging buffer
+ * per device (allocated by the first call on that device, which therefore
+ * must not be inside a stream capture), and one workspace serves one launch
+ * at a time on one stream. */
 int adrt_gb300_ragged_workspace_size(const int64_t *sizes, int64_t count, int dtype, size_t *bytes);
 int adrt_gb300_adrt_ragged(const void *in, void *out, const int64_t *sizes, int64_t count, int dtype,
                            void *workspace, size_t workspace_bytes, void *stream);
