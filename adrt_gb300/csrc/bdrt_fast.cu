@@ -354,6 +354,24 @@ __global__ void __launch_bounds__(NT, 2) pass1_kernel(const float *__restrict__ 
   if (c0 >= need + 31 * ap) return;
   const int kc = C - c0;
   const bool edge = kc < TWI;
+  if (kc <= 0) {
+    // The whole tile lies at frame positions >= 2n-1, where every input row
+    // reads +0 (a B row -0 only at its marker): an undone stage's outputs at
+    // u read inputs at >= u, and each is A + B with A = +0, so +0 (IEEE
+    // +0 + -0 = +0) at every level, and the final members, which get no
+    // marker, are +0.  Their stored offsets (u - a' i < 2n-1 for the members
+    // shifted that far) get +0 without loading or computing.
+    const float(&o)[4][4][4] = {};
+    float *rows_z = buf + ((size_t)bq * n + (size_t)ap * 32) * G::cs;
+    const int hz = threadIdx.x >> 5;
+    switch (ap & 3) {
+      case 0: pass1_store<0, NN>(o, rows_z, ap, c0, hz); break;
+      case 1: pass1_store<1, NN>(o, rows_z, ap, c0, hz); break;
+      case 2: pass1_store<2, NN>(o, rows_z, ap, c0, hz); break;
+      default: pass1_store<3, NN>(o, rows_z, ap, c0, hz); break;
+    }
+    return;
+  }
   const float *src = in + (size_t)bq * C * n + 32 * ap;
   // Stage the tile's 496 offsets x 32 angles (128-byte rows), chunk j of row
   // r at swizzled chunk j ^ ((r >> 3) & 7).  Offsets >= 2n-1 read +0, and
