@@ -85,3 +85,76 @@ def test_pass_a_decomposition_bit_exact(S):
                 for l in range(1 << GS):
                     got[st, (L1 << GS) + l] = w[l]
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def reference_bdrt_stages(buf, stages):
+    """The reference's transposed stages on [angles][sections][R]: angle
+    pair (2 si, 2 si + 1) of each section gives sections 2 sec (left, A + B)
+    and 2 sec + 1 (right[u] = A[u + si] + B[u + si + 1], a copy of A where
+    B's offset is R, +0 beyond).  src/adrt/adrt_cdefs_bdrt.hpp:56-116."""
+    for _ in range(stages):
+        H, S, R = buf.shape
+        out = np.empty((H // 2, 2 * S, R), dtype=buf.dtype)
+        for si in range(H // 2):
+            for sec in range(S):
+                A, B = buf[2 * si, sec], buf[2 * si + 1, sec]
+                out[si, 2 * sec] = A + B
+                right = np.zeros(R, dtype=buf.dtype)
+                if R - 1 - si > 0:
+                    right[: R - 1 - si] = A[si : R - 1] + B[si + 1 : R]
+                right[R - 1 - si] = A[R - 1]
+                out[si, 2 * sec + 1] = right
+        buf = out
+    return buf
+
+
+@pytest.mark.parametrize("n,ap", [(128, 0), (128, 3), (256, 5), (256, 7)])
+def test_bdrt_pass1_frame_bit_exact(n, ap):
+    # The register-level bdrt's first pass on input angle group a' (angles
+    # 32 a' .. 32 a' + 31), five stages undone with local shifts only, in one
+    # frame: row (member prefix p, step j) sits at reference offset F - a' p
+    # 2^(4-j); every row reads +0 past offset 2n-2 except a row in the B role,
+    # which reads -0 at exactly 2n-1 (so A + B copies A); member i is finally
+    # stored a' i to the left.  Also: every member value at frame positions
+    # >= 2n-1 is +0 (the tiles there store +0 without computing).
+    C = 2 * n - 1
+    rng = np.random.default_rng(n + ap)
+    y = rng.standard_normal((n, C)).astype(f32)  # [angle][offset] of one quadrant
+    y[rng.random(y.shape) < 0.05] = -0.0
+    y[:, C - 3 :] = np.where(rng.random((n, 3)) < 0.5, -0.0, y[:, C - 3 :])
+    want = reference_bdrt_stages(y[:, None, :].copy(), 5)  # [n/32 angles][32 sections][C]
+
+    E = C + 31 * ap + 64  # frame positions kept
+    rows = {}
+    for la in range(32):
+        r = np.zeros(E, dtype=f32)
+        r[:C] = y[32 * ap + la]
+        if la & 1:
+            r[C] = -0.0
+        rows[(0, la)] = r
+    for j in range(5):
+        new = {}
+        n_ang = 32 >> j
+        for (p, la) in rows:
+            if la & 1:
+                continue
+            li = la >> 1
+            A, B = rows[(p, la)], rows[(p, la + 1)]
+            left = A + B
+            right = np.zeros(E, dtype=f32)
+            right[: E - li - 1] = A[li : E - 1] + B[li + 1 : E]
+            new[(2 * p, li)] = left
+            new[(2 * p + 1, li)] = right
+        rows = new
+        # B rows of the next step: -0 at reference offset 2n-1
+        if j < 4:
+            for (p, la), r in rows.items():
+                if la & 1:
+                    r[C + ap * p * (1 << (4 - j))] = -0.0
+        assert len(rows) == 32 and n_ang // 2 * (2 << j) == 32
+    for i in range(32):
+        member = rows[(i, 0)]
+        got = member[ap * i : ap * i + C]
+        assert np.array_equal(got.view(np.uint32), want[ap, i].view(np.uint32)), i
+        beyond = member[C:]
+        assert np.all(beyond.view(np.uint32) == 0), i  # +0, not -0
