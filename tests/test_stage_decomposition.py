@@ -158,3 +158,104 @@ def test_bdrt_pass1_frame_bit_exact(n, ap):
         assert np.array_equal(got.view(np.uint32), want[ap, i].view(np.uint32)), i
         beyond = member[C:]
         assert np.all(beyond.view(np.uint32) == 0), i  # +0, not -0
+
+
+def iadrt_stage(x, s):
+    """One stage of the reference's exact inverse on [row][chain] planes
+    (x: (R, n)): chain (l, col), l < 2^(s+1), col < n / 2^(s+1), reads the
+    input chains E = (l/2, 2 col), O = E + 1 and runs from row R-1 down:
+      l even: v = (0 + E[r]) - O[r+1] + out[r+1]   (the last two if r+1 < R)
+      l odd:  v = (0 + O[r+d]) - E[r+d] (if r+d < R, else 0), d = 1 + col;
+              v += out[r+1] if r+1 < R.
+    src/adrt/adrt_cdefs_iadrt.hpp:53-105."""
+    R, n = x.shape
+    Cc = n >> s
+    C2 = Cc >> 1
+    out = np.empty_like(x)
+    z = x.dtype.type(0)
+    for l in range(2 << s):
+        for col in range(C2):
+            ch = l * C2 + col
+            e = (l >> 1) * Cc + 2 * col
+            o = e + 1
+            prev = z
+            for r in range(R - 1, -1, -1):
+                if l % 2 == 0:
+                    v = z + x[r, e]
+                    if r + 1 < R:
+                        v = v - x[r + 1, o]
+                        v = v + prev
+                else:
+                    d = 1 + col
+                    v = z
+                    if r + d < R:
+                        v = v + x[r + d, o]
+                        v = v - x[r + d, e]
+                    if r + 1 < R:
+                        v = v + prev
+                out[r, ch] = v
+                prev = v
+    return out
+
+
+def iadrt_last5_fused(x, s0):
+    """The fused kernel's sweep for stages s0 .. s0+4: one group of 32 chains
+    (indices 32A + lane at every level), rows from R-1 down, the five levels
+    in order at each row; each level reads the previous one at rows r, r+1
+    and r+d (d = 1 + col <= 16) from a 17-row ring."""
+    R, n = x.shape
+    z = x.dtype.type(0)
+    out = np.empty_like(x)
+    H = 17
+    for A in range(n >> 5):
+        ring = np.zeros((5, H, 32), dtype=x.dtype)
+        prev = [[z] * 32 for _ in range(5)]
+        for r in range(R - 1, -1, -1):
+            slot = r % H
+            ring[0, slot] = x[r, 32 * A:32 * A + 32]
+            for t in range(5):
+                vals = []
+                for lane in range(32):
+                    lam, col = lane >> (4 - t), lane & ((1 << (4 - t)) - 1)
+                    e = ((lam >> 1) << (5 - t)) + 2 * col
+                    o, d = e + 1, 1 + col
+                    if lam % 2 == 0:
+                        v = z + ring[t, slot, e]
+                        if r + 1 < R:
+                            v = v - ring[t, (r + 1) % H, o]
+                            v = v + prev[t][lane]
+                    else:
+                        v = z
+                        if r + d < R:
+                            assert d <= 16
+                            v = v + ring[t, (r + d) % H, o]
+                            v = v - ring[t, (r + d) % H, e]
+                        if r + 1 < R:
+                            v = v + prev[t][lane]
+                    prev[t][lane] = v
+                    vals.append(v)
+                if t < 4:
+                    ring[t + 1, slot] = vals
+                else:
+                    out[r, 32 * A:32 * A + 32] = vals
+    return out
+
+
+@pytest.mark.parametrize("n", [32, 64])
+def test_iadrt_fused_last5_equals_stages(oracle_mod, n):
+    # The staged restatement against the oracle's inverse, then the fused
+    # sweep against the staged one, bit for bit (float32, signed zeros).
+    rng = np.random.default_rng(n)
+    y = rng.standard_normal((4, 2 * n - 1, n)).astype(f32)
+    y[rng.random(y.shape) < 0.05] = -0.0
+    L = n.bit_length() - 1
+    staged = np.stack([y[q] for q in range(4)])
+    for s in range(L):
+        staged = np.stack([iadrt_stage(staged[q], s) for q in range(4)])
+    want = oracle_mod.iadrt(y)
+    assert np.array_equal(staged.view(np.uint32), want.view(np.uint32))
+    pre = np.stack([y[q] for q in range(4)])
+    for s in range(L - 5):
+        pre = np.stack([iadrt_stage(pre[q], s) for q in range(4)])
+    fused = np.stack([iadrt_last5_fused(pre[q], L - 5) for q in range(4)])
+    assert np.array_equal(fused.view(np.uint32), staged.view(np.uint32))
