@@ -259,3 +259,55 @@ def test_iadrt_fused_last5_equals_stages(oracle_mod, n):
         pre = np.stack([iadrt_stage(pre[q], s) for q in range(4)])
     fused = np.stack([iadrt_last5_fused(pre[q], L - 5) for q in range(4)])
     assert np.array_equal(fused.view(np.uint32), staged.view(np.uint32))
+
+
+def iadrt_stage_row_sweep(x, s):
+    """The single-stage kernel's odd chains swept by input row (stages with
+    C2 >= 32): a warp holds 32 consecutive columns of one odd l, lane lags
+    d0 + lane; at input row x each lane computes its output row x - d, into a
+    32-row ring; row x - d0 is stored once lane 0 has written it.  Even
+    chains as in the reference."""
+    R, n = x.shape
+    Cc = n >> s
+    C2 = Cc >> 1
+    assert C2 >= 32
+    out = iadrt_stage(x, s)  # even chains (and, for now, odd ones)
+    z = x.dtype.type(0)
+    for l in range(1, 2 << s, 2):
+        for col0 in range(0, C2, 32):
+            ring = np.full((32, 32), np.nan, dtype=x.dtype)
+            prev = [z] * 32
+            d0 = 1 + col0
+            stored = np.full((R, 32), np.nan, dtype=x.dtype)
+            for xr in range(R - 1 + d0 + 31, d0 - 1, -1):
+                for lane in range(32):
+                    d = d0 + lane
+                    y = xr - d
+                    if y < 0 or y >= R:
+                        continue
+                    if xr >= R:
+                        v = z  # rows R-d .. R-1: +0
+                    else:
+                        e = (l >> 1) * Cc + 2 * (col0 + lane)
+                        v = z + x[xr, e + 1]
+                        v = v - x[xr, e]
+                        v = v + prev[lane]
+                    prev[lane] = v
+                    ring[y & 31, lane] = v
+                yc = xr - d0
+                if yc < R:
+                    stored[yc] = ring[yc & 31]
+            chs = l * C2 + col0 + np.arange(32)
+            assert not np.isnan(stored).any()
+            out[:, chs] = stored
+    return out
+
+
+@pytest.mark.parametrize("n,s", [(64, 0), (128, 0), (128, 1)])
+def test_iadrt_row_sweep_equals_stage(n, s):
+    rng = np.random.default_rng(n + s)
+    x = rng.standard_normal((2 * n - 1, n)).astype(f32)
+    x[rng.random(x.shape) < 0.05] = -0.0
+    want = iadrt_stage(x, s)
+    got = iadrt_stage_row_sweep(x, s)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
