@@ -311,3 +311,22 @@ def test_iadrt_row_sweep_equals_stage(n, s):
     want = iadrt_stage(x, s)
     got = iadrt_stage_row_sweep(x, s)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_forward_support_is_plus_zero(n):
+    # After k stages a row at angle a is exactly +0 at offsets >= n + a (the
+    # padding's sums): the bound behind the intermediate's row length and
+    # pass B's zero tiles.  Inputs include -0 and NaN inside the image.
+    C = 2 * n - 1
+    rng = np.random.default_rng(n)
+    x = np.zeros((n, 1, C), dtype=f32)
+    x[:, 0, :n] = rng.standard_normal((n, n)).astype(f32)
+    x[:, 0, :n][rng.random((n, n)) < 0.05] = -0.0
+    x[n // 2, 0, n // 3] = np.nan
+    buf = x
+    for k in range(1, n.bit_length()):
+        buf = reference_stages(buf, 1)
+        for a in range(buf.shape[1]):
+            tail = buf[:, a, n + a:]
+            assert np.all(tail.view(np.uint32) == 0), (k, a)
